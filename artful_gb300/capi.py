@@ -1,0 +1,142 @@
+"""ctypes view of include/artful_cuda.h: struct layouts and the library's entry points.
+
+The product is the C ABI in libartful_cuda.so; this module only declares it for Python callers (the
+tests, bench.py).  Loading fails loudly when the library has not been built: there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libartful_cuda.so")
+
+MAP_WIDTH, MAP_HEIGHT = 2048, 1024
+DUST_WIDTH, DUST_HEIGHT = 1024, 256
+FLUID_WIDTH, FLUID_HEIGHT = 1024, 256
+COLORS = 256
+SKY_WIDTH, SKY_HEIGHT = 1024, 512
+ROWS_AT = MAP_WIDTH * MAP_HEIGHT
+COLORS_AT = ROWS_AT + MAP_HEIGHT * 2
+SKY_AT = COLORS_AT + COLORS * 3
+GLOW_AT = SKY_AT + SKY_WIDTH * SKY_HEIGHT
+DUST_AT = GLOW_AT + MAP_HEIGHT
+MAP_FLOATS = DUST_AT + DUST_WIDTH * DUST_HEIGHT
+FLUID_FLOATS = FLUID_WIDTH * FLUID_HEIGHT
+
+EXACT, FP32, FP64, MIXED = 0, 1, 2, 3
+PRECISIONS = {"exact": EXACT, "fp32": FP32, "fp64": FP64, "mixed": MIXED}
+
+END_HORIZON, END_SKY, END_OPAQUE, END_CAP, END_LIT = 0, 1, 2, 3, 0x10
+
+
+class Vec3(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", Vec3), ("target", Vec3), ("up", Vec3), ("fovY", C.c_float), ("near_", C.c_float)]
+
+
+class BlackHoleDesc(C.Structure):
+    _fields_ = [("position", Vec3), ("axis", Vec3)] + [
+        (n, C.c_float)
+        for n in ("mass", "spin", "discInner", "discOuter", "discHeight", "discThickness", "discGain", "doppler",
+                  "stars", "bloom", "exposure", "time", "shutter")
+    ] + [("velocity", Vec3), ("samples", C.c_int)]
+
+
+_F4 = C.c_float * 4
+_D4 = C.c_double * 4
+FRAME_FIELDS = ("er", "etheta", "ephi", "right", "up", "forward", "metric", "place", "spin", "flow", "boost", "disc",
+                "look", "image")
+
+
+class HoleFrame(C.Structure):
+    _fields_ = [(n, _F4) for n in FRAME_FIELDS] + [("size", C.c_uint32 * 4), ("bloom", (C.c_uint32 * 4) * 8)]
+
+
+class HoleFrame64(C.Structure):
+    _fields_ = [(n, _D4) for n in FRAME_FIELDS]
+
+
+class SynthDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("inner", C.c_float), ("outer", C.c_float), ("spin", C.c_float),
+                ("emissivity", C.c_float), ("stars", C.c_int)]
+
+
+class TraceOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("jitter", C.c_int), ("seed", C.c_uint32), ("stepScale", C.c_float),
+                ("horizonBand", C.c_float), ("blockSize", C.c_int), ("compactEvery", C.c_int),
+                ("persistent", C.c_int)]
+
+
+class RayEnd(C.Structure):
+    _fields_ = [("hitR", C.c_float), ("hitPhi", C.c_float), ("dir", C.c_float * 3), ("mino", C.c_float),
+                ("steps", C.c_uint16), ("crossings", C.c_uint8), ("kind", C.c_uint8),
+                ("fp64Steps", C.c_uint16), ("reserved", C.c_uint16)]
+
+
+class TraceStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("steps", C.c_uint64), ("crossings", C.c_uint64), ("escapes", C.c_uint64),
+                ("fp64Steps", C.c_uint64), ("flops", C.c_double), ("ms", C.c_float)]
+
+
+assert C.sizeof(HoleFrame) == 368 and C.sizeof(BlackHoleDesc) == 92 and C.sizeof(Camera) == 44
+assert C.sizeof(RayEnd) == 32
+
+P = C.POINTER
+_vp = C.c_void_p
+_fp = P(C.c_float)
+
+# name: (restype, argtypes)
+SIGNATURES = {
+    "artfCudaLastError": (C.c_char_p, []),
+    "artfCudaBlackHoleDefaults": (BlackHoleDesc, []),
+    "artfCudaIsco": (C.c_float, [C.c_float]),
+    "artfCudaOrbitSpeed": (C.c_float, [C.c_float, C.c_float]),
+    "artfCudaHoleClamp": (None, [P(BlackHoleDesc), P(BlackHoleDesc)]),
+    "artfCudaHoleFrame": (C.c_uint32, [P(Camera), P(BlackHoleDesc), C.c_double, C.c_int, C.c_int, P(HoleFrame)]),
+    "artfCudaHoleFrame64": (C.c_int, [P(Camera), P(BlackHoleDesc), C.c_double, C.c_int, C.c_int, P(HoleFrame64)]),
+    "artfCudaSetRings": (None, [_vp, C.c_float, C.c_float, C.c_float]),
+    "artfCudaSynthMap": (C.c_int, [P(SynthDesc), _vp]),
+    "artfCudaSynthRings": (None, [P(SynthDesc), _vp]),
+    "artfCudaCreate": (C.c_int, [C.c_int, P(_vp)]),
+    "artfCudaDestroy": (None, [_vp]),
+    "artfCudaSetMap": (C.c_int, [_vp, _vp, C.c_uint64]),
+    "artfCudaSetFluid": (C.c_int, [_vp, _vp, C.c_uint64]),
+    "artfCudaDeviceMap": (_vp, [_vp]),
+    "artfCudaDeviceFluid": (_vp, [_vp]),
+    "artfCudaStream": (_vp, [_vp]),
+    "artfCudaHoleTrace": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, _vp, P(TraceOptions), _vp, _vp,
+                                    P(TraceStats)]),
+    "artfCudaHoleRender": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, C.c_uint64, _vp, C.c_uint64,
+                                     P(TraceOptions), _vp, P(TraceStats)]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """The product library, with every declared entry point typed.  Raises when it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)  # AttributeError: the library lacks a declared symbol
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int, lib=None) -> None:
+    if status != 0:
+        lib = lib or load()
+        msg = lib.artfCudaLastError()
+        raise RuntimeError(f"artful_cuda status {status}: {msg.decode() if msg else ''}")

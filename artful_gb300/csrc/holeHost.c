@@ -1,0 +1,489 @@
+/* artful_cuda — the host side of the hole, in C11: what every frame's trace reads and that is the
+ * same for all of its rays.  A restatement of the reference's src/scene/hole.c for this path:
+ *
+ *   artfCudaBlackHoleDefaults  hole.c:225-240   artfCudaIsco       hole.c:199-213
+ *   artfCudaHoleClamp          hole.c:245-258   artfCudaOrbitSpeed hole.c:215-223
+ *   artfCudaHoleFrame          hole.c:273-371   artfCudaSetRings   hole.c:10-12, 186-197
+ *   colour table               hole.c:54-85, 159-164
+ *
+ * The FP32 frame keeps the reference's order of operations, with no contraction (this file is built
+ * with -ffp-contract=off), because the FP32 trace is checked bit for bit against the reference's.
+ * Nothing here calls exp, log or pow: the synthetic maps are made of integer hashing and IEEE
+ * + - * / sqrt, so that an x86 host and an Arm host write the same bits. */
+#include "artful_cuda.h"
+
+#include <math.h>
+#include <string.h>
+
+typedef ArtfCudaVec3 Vec;
+
+static Vec vec(float x, float y, float z) { Vec v = {x, y, z}; return v; }
+static Vec vsub(Vec a, Vec b) { return vec(a.x - b.x, a.y - b.y, a.z - b.z); }
+static Vec vscale(Vec a, float s) { return vec(a.x * s, a.y * s, a.z * s); }
+static float vdot(Vec a, Vec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static Vec vcross(Vec a, Vec b) { return vec(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static float vlength(Vec a) { return sqrtf(vdot(a, a)); }
+static Vec vnormalize(Vec a) {
+    const float l = vlength(a);
+    return l > 0 ? vscale(a, 1.f / l) : a;
+}
+/* (the reference's artfMinf / artfMaxf / artfClampf: which operand wins a tie or a NaN matters for bits) */
+static float fminRef(float a, float b) { return b < a ? b : a; }
+static float fmaxRef(float a, float b) { return a < b ? b : a; }
+static float fclampRef(float v, float lo, float hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+/* ---- orbits ------------------------------------------------------------------------------------- */
+
+/* x^(1/3) for x > 0 by Newton's iteration, 60 rounds from max(x, 1): converged to the last bit. */
+static double cubeRootNewton(double x) {
+    if (x <= 0) return 0;
+    double v = x > 1 ? x : 1;
+    for (int i = 0; i < 60; ++i) v = (2.0 * v + x / (v * v)) / 3.0;
+    return v;
+}
+
+/* Bardeen, Press & Teukolsky (1972): the ISCO radius of a Kerr hole, prograde for spin > 0. */
+float artfCudaIsco(float spin) {
+    const double a = spin, a2 = a * a;
+    const double z1 = 1.0 + cubeRootNewton(1.0 - a2) * (cubeRootNewton(1.0 + a) + cubeRootNewton(1.0 - a));
+    const double z2 = sqrt(3.0 * a2 + z1 * z1);
+    const double root = sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2));
+    return (float)(3.0 + z2 - (a < 0 ? -root : root));
+}
+
+/* A circular equatorial orbit's speed, measured by the zero-angular-momentum observer there. */
+float artfCudaOrbitSpeed(float spin, float r) {
+    const double a = spin, rr = (double)r * r, delta = rr - 2.0 * r + a * a;
+    const double big = (rr + a * a) * (rr + a * a) - a * a * delta;
+    const double omega = 1.0 / ((double)r * sqrt((double)r) + a), frameDrag = 2.0 * a * r / big;
+    const double varpi = sqrt(big) / r, lapse = r * sqrt(delta) / sqrt(big);
+    const double v = (omega - frameDrag) * varpi / lapse;
+    return (float)(v > .99 ? .99 : v);
+}
+
+/* ---- the description ------------------------------------------------------------------------------ */
+
+ArtfCudaBlackHoleDesc artfCudaBlackHoleDefaults(void) {
+    ArtfCudaBlackHoleDesc d;
+    memset(&d, 0, sizeof d);
+    d.axis = vec(0, -1, 0);
+    d.mass = 1.f;
+    d.spin = .6f;
+    d.discOuter = 34.f;
+    d.discHeight = .03f;
+    d.discThickness = 1.f;
+    d.discGain = 2.1f;
+    d.stars = .4f;
+    d.bloom = 4.5f;
+    d.exposure = 1.f;
+    d.samples = 1;
+    return d;
+}
+
+void artfCudaHoleClamp(const ArtfCudaBlackHoleDesc* in, ArtfCudaBlackHoleDesc* out) {
+    ArtfCudaBlackHoleDesc d = *in;
+    const float spin = fclampRef(in->spin, -.998f, .998f);
+    const float horizon = 1.f + sqrtf(1.f - spin * spin);
+    const float inner = in->discInner > 0 ? fmaxRef(in->discInner, horizon + .2f) : artfCudaIsco(spin);
+    d.spin = spin;
+    d.mass = fmaxRef(in->mass, 1e-6f);
+    d.discInner = inner;
+    d.discOuter = fmaxRef(in->discOuter, inner + 1.f);
+    d.discHeight = fmaxRef(in->discHeight, 1e-3f);
+    d.samples = in->samples < 1 ? 1 : in->samples > 8 ? 8 : in->samples;
+    *out = d;
+}
+
+/* ---- the frame ---------------------------------------------------------------------------------- */
+
+/* The disc's frame (x, y = axis, z) for a hole axis: its own basis, so that the disc lies in xz. */
+typedef struct DiscBasis { Vec ex, ey, ez; } DiscBasis;
+
+static DiscBasis discBasis(Vec axis) {
+    DiscBasis b;
+    const Vec given = vlength(axis) > 0 ? vnormalize(axis) : vec(0, 1, 0);
+    const Vec other = fabsf(given.z) < .9f ? vec(0, 0, 1) : vec(1, 0, 0);
+    b.ex = vnormalize(vcross(given, other));
+    b.ey = given;
+    b.ez = vcross(b.ex, b.ey);
+    return b;
+}
+
+/* A world vector in the eye's (r, theta, phi) directions: first into the disc frame in the trace's
+ * order (x, z, axis), then onto the three directions. */
+static void toLocal(Vec v, const DiscBasis* b, Vec er, Vec etheta, Vec ephi, float w, float* o) {
+    const Vec h = vec(vdot(v, b->ex), vdot(v, b->ez), vdot(v, b->ey));
+    o[0] = vdot(h, er);
+    o[1] = vdot(h, etheta);
+    o[2] = vdot(h, ephi);
+    o[3] = w;
+}
+
+static uint32_t bloomLevels(int width, int height, uint32_t (*bloom)[4], uint32_t* levelsOut) {
+    uint32_t w = (uint32_t)width, h = (uint32_t)height, at = 0, levels = 0;
+    while (levels < ARTF_CUDA_BLOOM_LEVELS && (!levels || (w > 3 && h > 3))) {
+        w = (w + 1) / 2;
+        h = (h + 1) / 2;
+        bloom[levels][0] = at;
+        bloom[levels][1] = w;
+        bloom[levels][2] = h;
+        at += w * h;
+        ++levels;
+    }
+    *levelsOut = levels;
+    return at;
+}
+
+uint32_t artfCudaHoleFrame(const ArtfCudaCamera* c, const ArtfCudaBlackHoleDesc* d, double fluidTime, int width,
+                           int height, ArtfCudaHoleFrame* out) {
+    if (!c || !d || !out || width < 1 || height < 1) return 0;
+    memset(out, 0, sizeof *out);
+    const float a = d->spin, horizon = 1.f + sqrtf(1.f - a * a);
+    const DiscBasis b = discBasis(d->axis);
+
+    /* the eye in masses, kept at least 0.3 above the horizon */
+    Vec eye = vscale(vsub(c->position, d->position), 1.f / d->mass);
+    float r = vlength(eye);
+    const float least = horizon + .3f;
+    if (r < least) {
+        eye = r > 0 ? vscale(eye, least / r) : vec(0, 0, least);
+        r = least;
+    }
+    const float px = vdot(eye, b.ex) / r, py = vdot(eye, b.ey) / r, pz = vdot(eye, b.ez) / r;
+    const float sine = sqrtf(px * px + pz * pz);
+    const float cx = sine > 1e-5f ? px / sine : 1.f, cz = sine > 1e-5f ? pz / sine : 0.f;
+    const Vec er = vec(px, pz, py), etheta = vec(py * cx, py * cz, -sine), ephi = vec(-cz, cx, 0);
+    out->er[0] = er.x, out->er[1] = er.y, out->er[2] = er.z, out->er[3] = r;
+    out->etheta[0] = etheta.x, out->etheta[1] = etheta.y, out->etheta[2] = etheta.z;
+    out->ephi[0] = ephi.x, out->ephi[1] = ephi.y, out->ephi[2] = ephi.z;
+
+    /* Kerr's metric at the eye, in Boyer-Lindquist form, for the observer at rest in the dragged frame */
+    const float mu = py, r2 = r * r, a2 = a * a;
+    const float sigma = r2 + a2 * mu * mu, delta = r2 - 2.f * r + a2;
+    const float big = (r2 + a2) * (r2 + a2) - a2 * delta * sine * sine;
+    const float rho = sqrtf(sigma), rootDelta = sqrtf(delta), rootBig = sqrtf(big);
+    const float varpiAxis = rootBig / rho;
+    out->metric[0] = rho * rootDelta / rootBig;
+    out->metric[1] = 2.f * a * r / big * varpiAxis * sine;
+    out->metric[2] = varpiAxis * sine;
+    out->metric[3] = varpiAxis;
+    out->place[0] = rho;
+    out->place[1] = rootDelta;
+    out->place[2] = 1.f / r;
+    out->place[3] = mu;
+    out->spin[0] = a;
+    out->spin[1] = .995f / horizon;
+    out->spin[2] = d->discHeight;
+    out->spin[3] = d->shutter;
+    out->flow[0] = (float)fluidTime;
+
+    /* the camera basis, scaled to the image's half extents, and the eye's velocity */
+    const Vec forward = vnormalize(vsub(c->target, c->position));
+    const Vec right = vnormalize(vcross(forward, c->up));
+    const Vec up = vcross(right, forward);
+    const float tanY = tanf(c->fovY * .5f), tanX = tanY * (float)width / (float)(height > 1 ? height : 1);
+    toLocal(vscale(right, tanX), &b, er, etheta, ephi, 0.f, out->right);
+    toLocal(vscale(up, tanY), &b, er, etheta, ephi, 0.f, out->up);
+    toLocal(forward, &b, er, etheta, ephi, 0.f, out->forward);
+    float speed = vlength(d->velocity);
+    const Vec velocity = speed > .99f ? vscale(d->velocity, .99f / speed) : d->velocity;
+    speed = fminRef(speed, .99f);
+    toLocal(velocity, &b, er, etheta, ephi, 1.f / sqrtf(1.f - speed * speed), out->boost);
+
+    out->disc[0] = d->discInner;
+    out->disc[1] = d->discOuter;
+    out->disc[2] = d->time;
+    out->disc[3] = d->discThickness;
+    out->look[0] = d->discGain;
+    out->look[1] = d->doppler;
+    out->look[2] = d->stars;
+    out->look[3] = d->bloom;
+    out->image[0] = d->exposure;
+    out->image[1] = 2.f / (float)width;
+    out->image[2] = 2.f / (float)height;
+    out->image[3] = 1.f / (float)(d->samples * d->samples);
+    out->size[0] = (uint32_t)width;
+    out->size[1] = (uint32_t)height;
+    out->size[2] = (uint32_t)d->samples;
+    return bloomLevels(width, height, out->bloom, &out->size[3]);
+}
+
+/* ---- the frame in double ---------------------------------------------------------------------- */
+
+typedef struct DVec { double x, y, z; } DVec;
+static DVec dvec(double x, double y, double z) { DVec v = {x, y, z}; return v; }
+static DVec dfrom(Vec v) { return dvec(v.x, v.y, v.z); }
+static DVec dsub(DVec a, DVec b) { return dvec(a.x - b.x, a.y - b.y, a.z - b.z); }
+static DVec dscale(DVec a, double s) { return dvec(a.x * s, a.y * s, a.z * s); }
+static double ddot(DVec a, DVec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static DVec dcross(DVec a, DVec b) { return dvec(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static double dlength(DVec a) { return sqrt(ddot(a, a)); }
+static DVec dnormalize(DVec a) {
+    const double l = dlength(a);
+    return l > 0 ? dscale(a, 1.0 / l) : a;
+}
+
+static void toLocal64(DVec v, const DVec* basis, DVec er, DVec etheta, DVec ephi, double w, double* o) {
+    const DVec h = dvec(ddot(v, basis[0]), ddot(v, basis[2]), ddot(v, basis[1]));
+    o[0] = ddot(h, er);
+    o[1] = ddot(h, etheta);
+    o[2] = ddot(h, ephi);
+    o[3] = w;
+}
+
+int artfCudaHoleFrame64(const ArtfCudaCamera* c, const ArtfCudaBlackHoleDesc* d, double fluidTime, int width,
+                        int height, ArtfCudaHoleFrame64* out) {
+    if (!c || !d || !out || width < 1 || height < 1) return ARTF_CUDA_EINVAL;
+    memset(out, 0, sizeof *out);
+    const double a = d->spin, horizon = 1.0 + sqrt(1.0 - a * a);
+    DVec basis[3];
+    {
+        const DVec axis = dfrom(d->axis);
+        const DVec given = dlength(axis) > 0 ? dnormalize(axis) : dvec(0, 1, 0);
+        const DVec other = fabs(given.z) < .9 ? dvec(0, 0, 1) : dvec(1, 0, 0);
+        basis[0] = dnormalize(dcross(given, other));
+        basis[1] = given;
+        basis[2] = dcross(basis[0], basis[1]);
+    }
+    DVec eye = dscale(dsub(dfrom(c->position), dfrom(d->position)), 1.0 / d->mass);
+    double r = dlength(eye);
+    const double least = horizon + .3;
+    if (r < least) {
+        eye = r > 0 ? dscale(eye, least / r) : dvec(0, 0, least);
+        r = least;
+    }
+    const double px = ddot(eye, basis[0]) / r, py = ddot(eye, basis[1]) / r, pz = ddot(eye, basis[2]) / r;
+    const double sine = sqrt(px * px + pz * pz);
+    const double cx = sine > 1e-5 ? px / sine : 1.0, cz = sine > 1e-5 ? pz / sine : 0.0;
+    const DVec er = dvec(px, pz, py), etheta = dvec(py * cx, py * cz, -sine), ephi = dvec(-cz, cx, 0);
+    out->er[0] = er.x, out->er[1] = er.y, out->er[2] = er.z, out->er[3] = r;
+    out->etheta[0] = etheta.x, out->etheta[1] = etheta.y, out->etheta[2] = etheta.z;
+    out->ephi[0] = ephi.x, out->ephi[1] = ephi.y, out->ephi[2] = ephi.z;
+    const double mu = py, r2 = r * r, a2 = a * a;
+    const double sigma = r2 + a2 * mu * mu, delta = r2 - 2.0 * r + a2;
+    const double big = (r2 + a2) * (r2 + a2) - a2 * delta * sine * sine;
+    const double rho = sqrt(sigma), rootDelta = sqrt(delta), rootBig = sqrt(big);
+    const double varpiAxis = rootBig / rho;
+    out->metric[0] = rho * rootDelta / rootBig;
+    out->metric[1] = 2.0 * a * r / big * varpiAxis * sine;
+    out->metric[2] = varpiAxis * sine;
+    out->metric[3] = varpiAxis;
+    out->place[0] = rho;
+    out->place[1] = rootDelta;
+    out->place[2] = 1.0 / r;
+    out->place[3] = mu;
+    out->spin[0] = a;
+    out->spin[1] = .995 / horizon;
+    out->spin[2] = d->discHeight;
+    out->spin[3] = d->shutter;
+    out->flow[0] = fluidTime;
+    const DVec forward = dnormalize(dsub(dfrom(c->target), dfrom(c->position)));
+    const DVec right = dnormalize(dcross(forward, dfrom(c->up)));
+    const DVec up = dcross(right, forward);
+    const double tanY = tan((double)c->fovY * .5), tanX = tanY * (double)width / (double)(height > 1 ? height : 1);
+    toLocal64(dscale(right, tanX), basis, er, etheta, ephi, 0, out->right);
+    toLocal64(dscale(up, tanY), basis, er, etheta, ephi, 0, out->up);
+    toLocal64(forward, basis, er, etheta, ephi, 0, out->forward);
+    DVec velocity = dfrom(d->velocity);
+    double speed = dlength(velocity);
+    if (speed > .99) velocity = dscale(velocity, .99 / speed);
+    if (speed > .99) speed = .99;
+    toLocal64(velocity, basis, er, etheta, ephi, 1.0 / sqrt(1.0 - speed * speed), out->boost);
+    out->disc[0] = d->discInner;
+    out->disc[1] = d->discOuter;
+    out->disc[2] = d->time;
+    out->disc[3] = d->discThickness;
+    out->look[0] = d->discGain;
+    out->look[1] = d->doppler;
+    out->look[2] = d->stars;
+    out->look[3] = d->bloom;
+    out->image[0] = d->exposure;
+    out->image[1] = 2.0 / width;
+    out->image[2] = 2.0 / height;
+    out->image[3] = 1.0 / ((double)d->samples * d->samples);
+    return ARTF_CUDA_OK;
+}
+
+/* ---- map tables ----------------------------------------------------------------------------- */
+
+/* Map rows are even in 1/r between inner (row 0) and outer (the last row). */
+static float rowRadius(float rho, float inner, float outer) { return inner / (1.f - rho * (1.f - inner / outer)); }
+
+#define DISC_KELVIN 4500.f  /* the disc's one temperature (the reference's HOLE_KELVIN) */
+#define TABLE_KELVIN 6500.0 /* heat 1 is this; the colour table's middle */
+
+static void ringSpeedHeat(float* map, float inner, float outer, float spin) {
+    float* rows = map + ARTF_CUDA_ROWS_AT;
+    for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
+        const float r = rowRadius((float)y / (float)(ARTF_CUDA_MAP_HEIGHT - 1), inner, outer);
+        rows[y * 2] = 1.f / (6.2831853f * (r * sqrtf(r) + spin));
+        rows[y * 2 + 1] = DISC_KELVIN / (float)TABLE_KELVIN;
+    }
+}
+
+void artfCudaSetRings(float* map, float inner, float outer, float spin) {
+    ringSpeedHeat(map, inner, outer, spin);
+    float* glow = map + ARTF_CUDA_GLOW_AT;
+    for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
+        const float r = rowRadius((float)y / (float)(ARTF_CUDA_MAP_HEIGHT - 1), inner, outer);
+        const float out = r / inner;
+        glow[y] = 6.f * out * sqrtf(out);
+    }
+}
+
+/* e^x as (1 + x / 2^20)^(2^20): multiplications only (the reference's exactExp). */
+static double expBySquaring(double x) {
+    double v = 1.0 + x / 1048576.0;
+    for (int i = 0; i < 20; ++i) v *= v;
+    return v;
+}
+
+/* Planck's spectral radiance at the three wavelengths that stand for a screen's primaries. */
+static void planckRgb(double kelvin, double* v) {
+    static const double metres[3] = {611e-9, 549e-9, 464e-9};
+    for (int c = 0; c < 3; ++c) {
+        const double l = metres[c], l2 = l * l;
+        v[c] = 1.0 / (l2 * l2 * l * (expBySquaring(.014388 / (l * kelvin)) - 1.0));
+    }
+}
+
+/* A black body's colour on film balanced so that 6500 K is white, brightest channel 1. */
+static void blackBodyRgb(double kelvin, float* rgb) {
+    double v[3], white[3], most = 0;
+    planckRgb(kelvin, v);
+    planckRgb(6500.0, white);
+    for (int c = 0; c < 3; ++c) {
+        v[c] /= white[c];
+        if (v[c] > most) most = v[c];
+    }
+    v[1] *= .6;
+    v[2] *= .72;
+    for (int c = 0; c < 3; ++c) rgb[c] = (float)(v[c] / most);
+}
+
+static void colourTable(float* map) {
+    float* colors = map + ARTF_CUDA_COLORS_AT;
+    for (int i = 0; i < ARTF_CUDA_COLORS; ++i) {
+        /* (through float, as the reference's artfMaxf takes it) */
+        const double kelvin = fmaxRef((float)(TABLE_KELVIN * (double)i / (ARTF_CUDA_COLORS / 2)), 400.f);
+        blackBodyRgb(kelvin, colors + i * 3);
+    }
+}
+
+/* ---- deterministic elementary functions (double, IEEE + - * / only) ------------------------------ */
+
+#define LN2 0.6931471805599453
+
+/* ln x for x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)), then 2 atanh((m - 1) / (m + 1)) by its series. */
+static double detLog(double x) {
+    int e = 0;
+    while (x >= 1.4142135623730951) { x *= .5; ++e; }
+    while (x < .7071067811865476) { x *= 2.0; --e; }
+    const double s = (x - 1.0) / (x + 1.0), s2 = s * s;
+    double term = s, sum = 0;
+    for (int k = 0; k < 30; ++k) {
+        sum += term / (double)(2 * k + 1);
+        term *= s2;
+    }
+    return 2.0 * sum + (double)e * LN2;
+}
+
+/* e^x: x = k ln 2 + t with |t| <= ln2 / 2, e^t by its Taylor series, times 2^k by halving or doubling. */
+static double detExp(double x) {
+    const double kf = floor(x / LN2 + .5);
+    const double t = x - kf * LN2;
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k < 28; ++k) {
+        term *= t / (double)k;
+        sum += term;
+    }
+    int k = (int)kf;
+    while (k > 0) { sum *= 2.0; --k; }
+    while (k < 0) { sum *= .5; ++k; }
+    return sum;
+}
+
+/* ---- the synthetic disc and sky -------------------------------------------------------------- */
+
+/* splitmix64's finaliser: a well-mixed 64-bit value of a 64-bit key. */
+static uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* A uniform value in [0, 1) with 24 bits, from a stream (seed, kind) at index i. */
+static double uniform24(uint64_t seed, uint64_t kind, uint64_t i) {
+    const uint64_t h = mix64(mix64(seed * 0x100000001B3ull ^ kind) ^ i);
+    return (double)(h >> 40) * (1.0 / 16777216.0);
+}
+
+#define LATTICE 64
+
+static float smoothWeight(float t) { return t * t * (3.f - 2.f * t); }
+
+/* The gas: value noise on a LATTICE x LATTICE grid over (azimuth, row), periodic in azimuth, each lattice
+ * value uniform in [0.5, 1.5], read between lattice points with smoothstep weights. */
+static void gasNoise(uint64_t seed, float* map) {
+    float lattice[LATTICE][LATTICE];
+    for (int j = 0; j < LATTICE; ++j)
+        for (int i = 0; i < LATTICE; ++i) lattice[j][i] = (float)(.5 + uniform24(seed, 1, (uint64_t)(j * LATTICE + i)));
+    for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
+        const float v = (float)y * ((float)(LATTICE - 1) / (float)(ARTF_CUDA_MAP_HEIGHT - 1));
+        int j0 = (int)v;
+        if (j0 > LATTICE - 2) j0 = LATTICE - 2;
+        const float ty = smoothWeight(v - (float)j0);
+        for (int x = 0; x < ARTF_CUDA_MAP_WIDTH; ++x) {
+            const float u = (float)x * ((float)LATTICE / (float)ARTF_CUDA_MAP_WIDTH);
+            const int i0 = (int)u % LATTICE, i1 = (i0 + 1) % LATTICE;
+            const float tx = smoothWeight(u - (float)(int)u);
+            const float top = lattice[j0][i0] + (lattice[j0][i1] - lattice[j0][i0]) * tx;
+            const float bottom = lattice[j0 + 1][i0] + (lattice[j0 + 1][i1] - lattice[j0 + 1][i0]) * tx;
+            map[(size_t)y * ARTF_CUDA_MAP_WIDTH + x] = top + (bottom - top) * ty;
+        }
+    }
+}
+
+void artfCudaSynthRings(const ArtfCudaSynthDesc* s, float* map) {
+    ringSpeedHeat(map, s->inner, s->outer, s->spin);
+    float* glow = map + ARTF_CUDA_GLOW_AT;
+    for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
+        const float r = rowRadius((float)y / (float)(ARTF_CUDA_MAP_HEIGHT - 1), s->inner, s->outer);
+        /* (r / inner)^-q */
+        glow[y] = (float)detExp(-(double)s->emissivity * detLog((double)r / (double)s->inner));
+    }
+}
+
+/* The sky: a floor of faint dust and a catalogue of point stars splatted between texels, so that the
+ * trace's bilinear read of the sky map finds each star where it is. */
+static void starSky(uint64_t seed, int stars, float* map) {
+    float* sky = map + ARTF_CUDA_SKY_AT;
+    for (int i = 0; i < ARTF_CUDA_SKY_WIDTH * ARTF_CUDA_SKY_HEIGHT; ++i) sky[i] = .0006f;
+    for (int s = 0; s < stars; ++s) {
+        const double height = 2.0 * uniform24(seed, 2, (uint64_t)s) - 1.0; /* uniform on the sphere */
+        const double turn = uniform24(seed, 3, (uint64_t)s);
+        const double brightness = detExp((-3.0 + 3.0 * uniform24(seed, 4, (uint64_t)s)) * 2.302585092994046);
+        const float at = (float)turn * (float)ARTF_CUDA_SKY_WIDTH;
+        const float rowAt = ((float)height * .5f + .5f) * (float)(ARTF_CUDA_SKY_HEIGHT - 1);
+        const int c0 = (int)at & (ARTF_CUDA_SKY_WIDTH - 1), c1 = (c0 + 1) & (ARTF_CUDA_SKY_WIDTH - 1);
+        int r0 = (int)rowAt;
+        if (r0 > ARTF_CUDA_SKY_HEIGHT - 2) r0 = ARTF_CUDA_SKY_HEIGHT - 2;
+        const float fx = at - (float)(int)at, fy = rowAt - (float)r0, b = (float)brightness;
+        sky[r0 * ARTF_CUDA_SKY_WIDTH + c0] += b * (1.f - fx) * (1.f - fy);
+        sky[r0 * ARTF_CUDA_SKY_WIDTH + c1] += b * fx * (1.f - fy);
+        sky[(r0 + 1) * ARTF_CUDA_SKY_WIDTH + c0] += b * (1.f - fx) * fy;
+        sky[(r0 + 1) * ARTF_CUDA_SKY_WIDTH + c1] += b * fx * fy;
+    }
+}
+
+int artfCudaSynthMap(const ArtfCudaSynthDesc* s, float* map) {
+    if (!s || !map || !(s->inner > 0) || !(s->outer > s->inner) || s->stars < 0) return ARTF_CUDA_EINVAL;
+    memset(map, 0, sizeof(float) * ARTF_CUDA_MAP_FLOATS);
+    gasNoise(s->seed, map);
+    artfCudaSynthRings(s, map);
+    colourTable(map);
+    starSky(s->seed, s->stars, map);
+    /* dust: none (the memset) */
+    return ARTF_CUDA_OK;
+}

@@ -1,0 +1,235 @@
+/* artful_cuda — Artful's Kerr black-hole tracer on one GB300 (sm_103a).
+ *
+ * The C ABI between a C11 host and the CUDA kernels.  Plain pointers and sizes only.  Every call
+ * returns 0 or a negative ArtfCudaStatus, and never aborts.  Pointers are borrowed for the call
+ * unless a comment says otherwise.
+ *
+ * What it replaces in the reference (eugeniobenfica/artful v0.4.0):
+ *   - the per-pixel trace `lensTrace` / `lensTile` of the software backend (src/software/lens.inc:99,
+ *     355) and the Vulkan hole compute shader (src/vulkan/shaders.c:1957 artfShaderHoleTrace), as
+ *     dispatched by `drawHole` (src/software/software.c:410-417) and `traceHole`
+ *     (src/vulkan/vulkan.c:1758-1781);
+ *   - the host set-up those read: `artfHoleFrame` (src/scene/hole.c:273), `artfHoleIsco` (hole.c:207),
+ *     `artfBlackHoleOrbitSpeed` (hole.c:215), `artfBlackHoleDefaults` (hole.c:225), the clamps of
+ *     `artfSceneSetBlackHole` (hole.c:242-258) and the ring tables of `setRings` (hole.c:186).
+ * The renderer backend that plugs all of this behind `artfRendererNew` is in artful_cuda_renderer.h. */
+#ifndef ARTFUL_CUDA_H
+#define ARTFUL_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ARTF_CUDA_ABI_VERSION 1
+
+/* ---- data layouts shared with the reference ----------------------------------------------------- */
+
+/* The map every backend reads, one block of floats (src/scene/sceneInternal.h:18-32, 324-329):
+ * painted gas 2048 x 1024 (rows even in 1/r), per row (turns per unit time, heat), black-body colours
+ * 256 x 3, sky dust 1024 x 512, per row glow, dust 1024 x 256.  The fluid is 1024 x 256. */
+#define ARTF_CUDA_MAP_WIDTH 2048
+#define ARTF_CUDA_MAP_HEIGHT 1024
+#define ARTF_CUDA_DUST_WIDTH 1024
+#define ARTF_CUDA_DUST_HEIGHT 256
+#define ARTF_CUDA_FLUID_WIDTH 1024
+#define ARTF_CUDA_FLUID_HEIGHT 256
+#define ARTF_CUDA_COLORS 256
+#define ARTF_CUDA_SKY_WIDTH 1024
+#define ARTF_CUDA_SKY_HEIGHT 512
+#define ARTF_CUDA_BLOOM_LEVELS 8
+#define ARTF_CUDA_ROWS_AT (ARTF_CUDA_MAP_WIDTH * ARTF_CUDA_MAP_HEIGHT)
+#define ARTF_CUDA_COLORS_AT (ARTF_CUDA_ROWS_AT + ARTF_CUDA_MAP_HEIGHT * 2)
+#define ARTF_CUDA_SKY_AT (ARTF_CUDA_COLORS_AT + ARTF_CUDA_COLORS * 3)
+#define ARTF_CUDA_GLOW_AT (ARTF_CUDA_SKY_AT + ARTF_CUDA_SKY_WIDTH * ARTF_CUDA_SKY_HEIGHT)
+#define ARTF_CUDA_DUST_AT (ARTF_CUDA_GLOW_AT + ARTF_CUDA_MAP_HEIGHT)
+#define ARTF_CUDA_MAP_FLOATS (ARTF_CUDA_DUST_AT + ARTF_CUDA_DUST_WIDTH * ARTF_CUDA_DUST_HEIGHT)
+#define ARTF_CUDA_FLUID_FLOATS (ARTF_CUDA_FLUID_WIDTH * ARTF_CUDA_FLUID_HEIGHT)
+
+/* Layout-compatible with the reference's public ArtfVec3 and ArtfCamera (include/artful/core.h,
+ * include/artful/scene.h:314-320). */
+typedef struct ArtfCudaVec3 { float x, y, z; } ArtfCudaVec3;
+typedef struct ArtfCudaCamera {
+    ArtfCudaVec3 position, target, up;
+    float fovY;  /* radians */
+    float near_;
+} ArtfCudaCamera;
+
+/* Layout-compatible with the reference's ArtfBlackHoleDesc (include/artful/scene.h:470-490). */
+typedef struct ArtfCudaBlackHoleDesc {
+    ArtfCudaVec3 position, axis;
+    float mass, spin, discInner, discOuter, discHeight, discThickness, discGain, doppler, stars, bloom, exposure,
+        time, shutter;
+    ArtfCudaVec3 velocity;
+    int samples;
+} ArtfCudaBlackHoleDesc;
+
+/* Per-frame constants, the reference's uniform block (src/scene/sceneInternal.h:302-319): 368 bytes. */
+typedef struct ArtfCudaHoleFrame {
+    float er[4];      /* the eye on the unit sphere in the disc frame (x, z, axis); w: its distance */
+    float etheta[4], ephi[4];
+    float right[4], up[4], forward[4]; /* a pixel's ray along (r, theta, phi) at the eye */
+    float metric[4];  /* lapse, frame-drag rate times radius, that radius, radius per sine */
+    float place[4];   /* sqrt(Sigma), sqrt(Delta), 1/r, cos(theta) */
+    float spin[4];    /* a, 0.995 / r+, disc height, shutter */
+    float flow[4];    /* the moment the fluid field is of */
+    float boost[4];   /* eye velocity along (r, theta, phi); w: gamma */
+    float disc[4];    /* inner, outer, time, thickness */
+    float look[4];    /* gain, doppler, stars, bloom */
+    float image[4];   /* exposure, 2/width, 2/height, 1/rays a pixel */
+    uint32_t size[4]; /* width, height, rays a side, bloom levels */
+    uint32_t bloom[ARTF_CUDA_BLOOM_LEVELS][4];
+} ArtfCudaHoleFrame;
+
+/* The same constants computed in double from the same description (no reference counterpart: the
+ * reference fills its frame in FP32).  The FP64 and mixed-precision traces read it. */
+typedef struct ArtfCudaHoleFrame64 {
+    double er[4], etheta[4], ephi[4], right[4], up[4], forward[4], metric[4], place[4], spin[4], flow[4], boost[4],
+        disc[4], look[4], image[4];
+} ArtfCudaHoleFrame64;
+
+/* ---- status ------------------------------------------------------------------------------------- */
+
+typedef enum ArtfCudaStatus {
+    ARTF_CUDA_OK = 0,
+    ARTF_CUDA_EINVAL = -1,     /* a NULL pointer, a size out of range, an unknown option */
+    ARTF_CUDA_ENODEVICE = -2,  /* no sm_103 device, or the device asked for does not exist */
+    ARTF_CUDA_ENOMEM = -3,     /* a device allocation failed */
+    ARTF_CUDA_ELAUNCH = -4,    /* a launch or copy failed; the context should be destroyed */
+    ARTF_CUDA_ETIMEOUT = -5,   /* a bounded device wait gave up (the persistent queue) */
+    ARTF_CUDA_ELOST = -6       /* the context was marked lost (a fault injected on the host) */
+} ArtfCudaStatus;
+
+/* A line about the last error of this thread's calls; borrowed. */
+const char* artfCudaLastError(void);
+
+/* ---- host set-up: the reference's hole.c, restated (C11, no GPU needed) ------------------------- */
+
+/* hole.c:225 artfBlackHoleDefaults */
+ArtfCudaBlackHoleDesc artfCudaBlackHoleDefaults(void);
+/* hole.c:207 artfHoleIsco: the innermost stable circular orbit, in masses */
+float artfCudaIsco(float spin);
+/* hole.c:215 artfBlackHoleOrbitSpeed */
+float artfCudaOrbitSpeed(float spin, float r);
+/* The clamps artfSceneSetBlackHole applies (hole.c:245-258): spin to +-0.998, inner to the ISCO when 0 or
+ * at least r+ + 0.2, outer at least inner + 1, height at least 1e-3, samples 1..8, mass at least 1e-6. */
+void artfCudaHoleClamp(const ArtfCudaBlackHoleDesc* in, ArtfCudaBlackHoleDesc* out);
+/* hole.c:273 artfHoleFrame for a clamped description, the camera, and the moment the fluid field is of.
+ * Returns the bloom pixel count; 0 on a bad argument. */
+uint32_t artfCudaHoleFrame(const ArtfCudaCamera* camera, const ArtfCudaBlackHoleDesc* clamped, double fluidTime,
+                           int width, int height, ArtfCudaHoleFrame* out);
+/* The same frame in double (for the FP64 and mixed traces). Returns 0, or ARTF_CUDA_EINVAL. */
+int artfCudaHoleFrame64(const ArtfCudaCamera* camera, const ArtfCudaBlackHoleDesc* clamped, double fluidTime,
+                        int width, int height, ArtfCudaHoleFrame64* out);
+/* hole.c:186 setRings: per map row its orbit speed and heat, and its glow (the reference's painted disc). */
+void artfCudaSetRings(float* map, float inner, float outer, float spin);
+
+/* The synthetic disc and sky of the benchmark configurations, written into a whole map.
+ *   gas:   value noise on a 64 x 64 lattice in (radius row, azimuth), seeded, in [0.5, 1.5];
+ *   glow:  (r / inner)^-emissivity, so the emission falls as r^-q;
+ *   rows:  the reference's orbit speed and heat (hole.c:186-192);
+ *   colours: the reference's black-body table (hole.c:159-164);
+ *   sky:   a floor of 0.0006 plus `stars` point stars, uniform on the sphere, brightness log-uniform in
+ *          [1e-3, 1], splatted bilinearly;  dust: none.
+ * Every value comes from integer hashing and IEEE + - * / sqrt only: the same bits on every host. */
+typedef struct ArtfCudaSynthDesc {
+    uint64_t seed;
+    float inner, outer, spin;  /* the clamped disc */
+    float emissivity;          /* q */
+    int stars;                 /* how many catalogue stars: 2000 in the benchmarks */
+} ArtfCudaSynthDesc;
+int artfCudaSynthMap(const ArtfCudaSynthDesc* desc, float* map);
+/* Only the rows and glow of a synthetic map (what changes with spin, inner and q). */
+void artfCudaSynthRings(const ArtfCudaSynthDesc* desc, float* map);
+
+/* ---- device context ------------------------------------------------------------------------------ */
+
+typedef struct ArtfCuda ArtfCuda;
+
+/* Opens `device` (an sm_103 GPU) and its stream; owns the device copies of the map and fluid. */
+int artfCudaCreate(int device, ArtfCuda** out);
+void artfCudaDestroy(ArtfCuda* ctx);
+/* Copies a whole map (ARTF_CUDA_MAP_FLOATS) / fluid field (ARTF_CUDA_FLUID_FLOATS) from the host when
+ * `version` differs from the one held (0 always copies). */
+int artfCudaSetMap(ArtfCuda* ctx, const float* hostMap, uint64_t version);
+int artfCudaSetFluid(ArtfCuda* ctx, const float* hostFluid, uint64_t version);
+/* The device copies, for callers that launch on their own buffers. */
+const float* artfCudaDeviceMap(const ArtfCuda* ctx);
+const float* artfCudaDeviceFluid(const ArtfCuda* ctx);
+/* The context's stream (a cudaStream_t). */
+void* artfCudaStream(const ArtfCuda* ctx);
+
+/* ---- the trace ----------------------------------------------------------------------------------- */
+
+typedef enum ArtfCudaPrecision {
+    ARTF_CUDA_EXACT = 0,  /* FP32 with the reference's rounding (no contraction, IEEE / and sqrt): the same
+                           * bits as the software backend */
+    ARTF_CUDA_FP32 = 1,   /* FP32 with fused multiply-adds and fast reciprocals */
+    ARTF_CUDA_FP64 = 2,   /* plain FP64 throughout, from the FP64 frame */
+    ARTF_CUDA_MIXED = 3   /* FP32 steps; FP64 constants of motion, turning-point and near-horizon steps */
+} ArtfCudaPrecision;
+
+typedef struct ArtfCudaTraceOptions {
+    int precision;       /* ArtfCudaPrecision */
+    int jitter;          /* 0: the reference's side x side stratified samples (frame size[2]);
+                          * n > 0: n rays a pixel at seeded uniform sub-pixel offsets */
+    uint32_t seed;       /* of the jitter */
+    float stepScale;     /* 1: the reference's step (pi/24 / sqrt(max(K, 4))); 0.5: half steps, with twice
+                          * the step cap. 0 means 1 */
+    float horizonBand;   /* mixed: FP64 steps where u > band * (0.995 / r+); 0 means the default (0.5) */
+    int blockSize;       /* threads a block: 0 picks the tuned value */
+    int compactEvery;    /* steps between warp refills: 0 picks the tuned value */
+    int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */
+} ArtfCudaTraceOptions;
+
+/* Endpoint of each ray (optional output), 32 bytes. */
+typedef struct ArtfCudaRayEnd {
+    float hitR, hitPhi;  /* first lit disc crossing: radius in masses, azimuth in turns [0, 1); NaN: none */
+    float dir[3];        /* escape direction, after the frame-drag rotation; 0: did not escape */
+    float mino;          /* the Mino time at the endpoint */
+    uint16_t steps;      /* integration steps taken */
+    uint8_t crossings;   /* accepted disc crossings */
+    uint8_t kind;        /* ARTF_CUDA_END_*, | ARTF_CUDA_END_LIT when a crossing gave light */
+    uint16_t fp64Steps;  /* of those, how many ran in FP64 (the mixed trace) */
+    uint16_t reserved;
+} ArtfCudaRayEnd;
+
+enum {
+    ARTF_CUDA_END_HORIZON = 0,  /* fell through 0.995 r+ */
+    ARTF_CUDA_END_SKY = 1,      /* escaped (u < 0) */
+    ARTF_CUDA_END_OPAQUE = 2,   /* the disc let through 0.004 or less */
+    ARTF_CUDA_END_CAP = 3,      /* ran out of steps */
+    ARTF_CUDA_END_LIT = 0x10
+};
+
+/* Pixel classes written into the alpha of each HDR pixel: bit 0 a ray was lit by the disc, bit 1 a ray
+ * escaped, bit 2 a ray ended dark (horizon, cap or opaque). */
+
+/* What a trace did, counted on the device. */
+typedef struct ArtfCudaTraceStats {
+    uint64_t rays, steps, crossings, escapes, fp64Steps;
+    double flops;        /* algorithmic FP32-pipe operations (the counting rule is in lensFlops.h) */
+    float ms;            /* device time of the trace kernel(s), CUDA events on the context's stream */
+} ArtfCudaTraceStats;
+
+/* Traces one frame into `hdr` (device memory, width * height float4: linear RGB and the class bits).
+ * map, fluid: device pointers (NULL: the context's copies).  frame64: needed for FP64 and MIXED (NULL:
+ * promoted from `frame`).  ends: device memory for width * height * rays-a-pixel records, or NULL.
+ * stats: filled when not NULL (it synchronises the stream).  Asynchronous otherwise. */
+int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
+                      const float* map, const float* fluid, const ArtfCudaTraceOptions* options, float* hdr,
+                      ArtfCudaRayEnd* ends, ArtfCudaTraceStats* stats);
+
+/* The same from host memory to host memory: copies the map and fluid (when their versions changed),
+ * traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */
+int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
+                       const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
+                       const ArtfCudaTraceOptions* options, float* hostHdr, ArtfCudaTraceStats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
