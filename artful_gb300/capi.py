@@ -112,6 +112,9 @@ SIGNATURES = {
                                     P(TraceStats)]),
     "artfCudaHoleRender": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, C.c_uint64, _vp, C.c_uint64,
                                      P(TraceOptions), _vp, P(TraceStats)]),
+    "artfCudaHoleTraceRays": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, _vp, C.c_int, C.c_float, C.c_int,
+                                        _vp, _vp, _vp, _vp, _vp, P(TraceStats)]),
+    "artfCudaProbePeaks": (C.c_int, [_vp, C.c_int, P(C.c_double), P(C.c_double)]),
 }
 
 _lib = None

@@ -1,0 +1,45 @@
+/* artful_cuda — what the C ABI (abi.cu) hands the kernel translation units: one struct of launch
+ * parameters, and one launcher per precision, each in its own .cu with its own float flags. */
+#pragma once
+
+#include "artful_cuda.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace artf {
+
+/* Device counters a trace adds to (unsigned 64-bit each). */
+enum Counter { CRays, CSteps, CCrossings, CEscapes, CFp64Steps, CQueue, CStatus, CCount };
+
+struct TraceLaunch {
+    ArtfCudaHoleFrame frame;      /* the FP32 frame (sample positions always come from it) */
+    ArtfCudaHoleFrame64 frame64;  /* the FP64 frame (FP64 and mixed traces) */
+    const float* map;
+    const float* fluid;
+    float4* hdr;                  /* width * height */
+    ArtfCudaRayEnd* ends;         /* width * height * rays, or NULL */
+    unsigned long long* counters; /* CCount of them, zeroed by the caller */
+    int jitter;
+    uint32_t seed;
+    float stepScale;
+    float horizonBand;
+    int blockSize;
+    int compactEvery;
+    int persistent;
+    int smCount;
+    cudaStream_t stream;
+    /* a list of rays in place of a frame's pixels (rayCount > 0) */
+    int rayCount;
+    const float* rayX;
+    const float* rayY;
+    const float* rayTime;
+    float* rayRgb;
+};
+
+cudaError_t launchExact(const TraceLaunch& l);
+cudaError_t launchFast(const TraceLaunch& l);
+cudaError_t launchFp64(const TraceLaunch& l);
+cudaError_t launchMixed(const TraceLaunch& l);
+
+}  // namespace artf

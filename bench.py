@@ -1,0 +1,351 @@
+"""Benchmark of the Kerr hole trace on GB300: geodesics/s at 1080p.
+
+The headline is the mixed-precision trace of the 1920 x 1080, 4-jittered-rays-a-pixel view (a = 0.998,
+r_obs = 50 M, i = 85 deg), next to the plain FP64 trace of the same frame (the ratio is the target's
+4x), each with its endpoint error against FP64 at half step.  A step is one trace of the whole frame
+(8,294,400 geodesics) with the inputs resident in HBM; L2 is flushed (a 256 MB write) before every timed
+step, outside the timed region.  `e2e` is the same metric through the host-buffer C ABI call
+(artfCudaHoleRender): the map and fluid copied from pinned host memory and the HDR frame copied back,
+every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU path on this host's cores: the oracle port (the reference's
+own sources are not on this machine), with all host threads, on a bounded sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "geodesics/s @1080p: mixed-prec vs FP64 GPU at ≤1e-4 endpoint err; adj/fwd time"
+UNIT = "geodesics/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--quick", action="store_true", help="skip the slow side measurements")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons while the timed region runs."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, frame, map_, fluid, jitter, budget_s=12.0):
+    """The oracle port on all host threads: rows of the same frame, as many as fit the budget."""
+    from oracle import binding
+    threads = binding.oracle().oracleThreads()
+    rows = 8
+    t0 = time.perf_counter()
+    binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads, rows=(536, 544))
+    dt = time.perf_counter() - t0
+    rays_per_s = rows * scene.width * jitter / dt
+    total = int(min(scene.height, max(8, budget_s * rays_per_s / (scene.width * jitter))))
+    y0 = max(0, scene.height // 2 - total // 2)
+    t0 = time.perf_counter()
+    binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads,
+                     rows=(y0, y0 + total))
+    dt = time.perf_counter() - t0
+    return {"value": total * scene.width * jitter / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"rows {y0}..{y0 + total} of the 1920x1080 frame, {jitter} jittered rays a pixel "
+                      f"({total * scene.width * jitter} geodesics, {dt:.1f} s); the oracle port, scalar C, "
+                      f"{threads} threads"}
+
+
+def run_reference(args, rank, world):
+    from artful_gb300 import capi, scenes
+    if rank != 0:
+        return
+    scene = scenes.config2(4)
+    frame, frame64, clamped = scenes.frame(scene)
+    map_ = scenes.synth_map(capi.load(), clamped, scene.seed, scene.emissivity)
+    fluid = scenes.unit_fluid()
+    from oracle import binding
+    threads = binding.oracle().oracleThreads()
+    rows = 16
+    values = []
+    for k in range(args.warmup + args.steps):
+        y0 = (k * rows * 7) % (scene.height - rows)
+        t0 = time.perf_counter()
+        binding.render32(frame, map_, fluid, jitter=4, seed=scene.jitter_seed, threads=threads, rows=(y0, y0 + rows))
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            values.append(rows * scene.width * 4 / dt)
+    value = statistics.median(values)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows * scene.width * 4 / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50, i=85",
+                       "sample_per_step": f"{rows} rows x 1920 x 4 rays"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{rows} rows of the frame a step; the reference's sources are not on "
+                                       "this host, so its algorithm runs as the oracle port (scalar C)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    from artful_gb300 import capi, scenes
+    torch.cuda.set_device(local)
+    lib = capi.load()
+    ctx = C.c_void_p()
+    capi.check(lib.artfCudaCreate(local, C.byref(ctx)))
+    stream = torch.cuda.ExternalStream(lib.artfCudaStream(ctx), device=f"cuda:{local}")
+
+    scene = scenes.config2(4)
+    frame, frame64, clamped = scenes.frame(scene)
+    map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    fluid = scenes.unit_fluid()
+    capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
+    capi.check(lib.artfCudaSetFluid(ctx, fluid.ctypes.data, 1))
+    w, h, rays = scene.width, scene.height, 4
+    geodesics = w * h * rays
+    hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def opts(precision, step_scale=1.0):
+        return capi.TraceOptions(precision, rays, scene.jitter_seed, step_scale, 0.0, 0, 0, 0)
+
+    def timed(precision, steps, warmup):
+        o = opts(precision)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                                                 hdr.data_ptr(), None, None))
+            stream.synchronize()
+            barrier(world)
+            total = 0.0
+            for _ in range(steps):
+                flush.fill_(1)
+                start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                start.record(stream)
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                                                 hdr.data_ptr(), None, None))
+                stop.record(stream)
+                stop.synchronize()
+                total += start.elapsed_time(stop)
+            torch.cuda.synchronize()
+            barrier(world)
+        return max_over_ranks(total / steps, world)
+
+    def stats_of(precision):
+        s = capi.TraceStats()
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts(precision)),
+                                         hdr.data_ptr(), None, C.byref(s)))
+        return s
+
+    # the headline: mixed precision, timed (clocks sampled meanwhile)
+    with Clocks(local) as clocks:
+        ms_mixed = timed(capi.MIXED, args.steps, args.warmup)
+    s_mixed = stats_of(capi.MIXED)
+    side = {}
+    fp64_steps = max(2, args.steps // 3)
+    ms_fp64 = timed(capi.FP64, fp64_steps, 1)
+    side["fp64"] = {"geodesics_per_s": geodesics / (ms_fp64 * 1e-3), "ms_per_frame": ms_fp64}
+    for name, prec in (("fp32_exact", capi.EXACT), ("fp32_fast", capi.FP32)):
+        ms = timed(prec, args.steps, 1)
+        s = stats_of(prec)
+        side[name] = {"geodesics_per_s": geodesics / (ms * 1e-3), "ms_per_frame": ms,
+                      "steps_per_s": s.steps / (ms * 1e-3)}
+
+    # endpoint error of the mixed trace: against FP64 at the same step (precision) and at half step
+    # (precision and discretisation), over every ray of the frame
+    def ends_of(precision, step_scale=1.0):
+        e = torch.empty((geodesics * 32,), dtype=torch.uint8, device="cuda")
+        o = opts(precision, step_scale)
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                                         hdr.data_ptr(), e.data_ptr(), None))
+        torch.cuda.synchronize()
+        from oracle.binding import END_DTYPE
+        return np.frombuffer(e.cpu().numpy().tobytes(), END_DTYPE), hdr.cpu().numpy().copy()
+
+    endpoint = {}
+    if not args.quick:
+        e_mixed, img_mixed = ends_of(capi.MIXED)
+        for label, scale in (("vs_fp64_same_step", 1.0), ("vs_fp64_half_step", 0.5)):
+            e_ref, img_ref = ends_of(capi.FP64, scale)
+            endpoint[label] = endpoint_error(e_mixed, e_ref, img_mixed, img_ref)
+
+    # roofline of the trace: the FP32 pipe (the dominant kernel is FP32-bound; no tensor cores)
+    fp32_peak, fp64_peak = C.c_double(), C.c_double()
+    capi.check(lib.artfCudaProbePeaks(lib.artfCudaStream(ctx), local, C.byref(fp32_peak), C.byref(fp64_peak)))
+    achieved = s_mixed.flops / (ms_mixed * 1e-3) / 1e12
+    peak = fp32_peak.value / 1e12
+
+    # end to end through the host-buffer entry point
+    pin_map = torch.from_numpy(map_).pin_memory()
+    pin_fluid = torch.from_numpy(fluid).pin_memory()
+    pin_hdr = torch.empty((h, w, 4), dtype=torch.float32).pin_memory()
+    o = opts(capi.MIXED)
+    for _ in range(args.warmup):
+        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), C.byref(frame64), pin_map.data_ptr(), 0,
+                                          pin_fluid.data_ptr(), 0, C.byref(o), pin_hdr.data_ptr(), None))
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), C.byref(frame64), pin_map.data_ptr(), 0,
+                                          pin_fluid.data_ptr(), 0, C.byref(o), pin_hdr.data_ptr(), None))
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+
+    cpu = None
+    if rank == 0 and not args.quick:
+        cpu = cpu_baseline(scene, frame, map_, fluid, rays)
+
+    lib.artfCudaDestroy(ctx)
+    if rank != 0:
+        return
+    value = world * geodesics / (ms_mixed * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50 M, i=85 deg, "
+                               "disc ISCO..12 M r^-3, 2000 stars", "precision": "mixed",
+                   "parallelism": f"replicas{world}", "l2": "flushed (256 MB write) before every timed step"},
+        "mixed_over_fp64": side["fp64"]["ms_per_frame"] / ms_mixed,
+        "steps_per_s": s_mixed.steps / (ms_mixed * 1e-3) * world,
+        "fp64_step_share": s_mixed.fp64Steps / max(1, s_mixed.steps),
+        "side": side,
+        "endpoint_error": endpoint,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured FMA-chain probe (artfCudaProbePeaks); MEASURED_PEAKS.json has no "
+                                    "FP32-pipe figure",
+                     "fp64_peak_tflops": fp64_peak.value / 1e12,
+                     "flops_per_frame": s_mixed.flops},
+        "e2e": {"value": world * geodesics / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": (map_.nbytes + fluid.nbytes), "d2h_bytes_per_step": h * w * 16},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def endpoint_error(e, r, img, img_ref):
+    """Relative endpoint error of each ray against a reference trace: disc-hit radius and azimuth, escape
+    direction, and the pixel's radiance."""
+    both_hit = np.isfinite(e["hitR"]) & np.isfinite(r["hitR"])
+    dr = np.abs(e["hitR"][both_hit] - r["hitR"][both_hit]) / r["hitR"][both_hit]
+    dphi = np.abs(e["hitPhi"][both_hit] - r["hitPhi"][both_hit])
+    dphi = np.minimum(dphi, 1 - dphi)  # turns, on the circle
+    both_sky = ((e["kind"] & 15) == 1) & ((r["kind"] & 15) == 1)
+    ddir = np.linalg.norm(e["dir"][both_sky] - r["dir"][both_sky], axis=1)
+    same_kind = np.mean((e["kind"] & 15) == (r["kind"] & 15))
+    lum = img[..., :3].astype(np.float64).sum(-1)
+    lum_ref = img_ref[..., :3].astype(np.float64).sum(-1)
+    drad = np.abs(lum - lum_ref) / np.maximum(lum_ref, 1e-3)
+    per_ray = np.zeros(len(e))
+    per_ray[both_hit] = np.maximum(dr, dphi)
+    per_ray[both_sky] = np.maximum(per_ray[both_sky], ddir)
+    comparable = both_hit | both_sky
+    q = lambda a, p: float(np.quantile(a, p)) if len(a) else None  # noqa: E731
+    return {
+        "rays_within_1e-4": float(np.mean(per_ray[comparable] <= 1e-4)),
+        "same_end_kind": float(same_kind),
+        "hit_r_rel": {"median": q(dr, .5), "p99": q(dr, .99)},
+        "hit_phi_turns": {"median": q(dphi, .5), "p99": q(dphi, .99)},
+        "escape_dir": {"median": q(ddir, .5), "p99": q(ddir, .99)},
+        "radiance_rel": {"median": q(drad.ravel(), .5), "p99": q(drad.ravel(), .99),
+                         "pixels_within_1e-3": float(np.mean(drad <= 1e-3))},
+    }
+
+
+if __name__ == "__main__":
+    main()

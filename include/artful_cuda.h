@@ -222,11 +222,25 @@ int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfC
                       const float* map, const float* fluid, const ArtfCudaTraceOptions* options, float* hdr,
                       ArtfCudaRayEnd* ends, ArtfCudaTraceStats* stats);
 
+/* Traces n rays at given image positions and moments (device arrays of n floats each) into rgb (device,
+ * 3 floats a ray): the per-ray form of the reference's trace (src/software/lens.inc:99 lensTrace), for
+ * callers that make their own sample positions.  precision: ArtfCudaPrecision.  ends may be NULL. */
+int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
+                          const float* map, const float* fluid, int precision, float stepScale, int n, const float* nx,
+                          const float* ny, const float* time, float* rgb, ArtfCudaRayEnd* ends,
+                          ArtfCudaTraceStats* stats);
+
 /* The same from host memory to host memory: copies the map and fluid (when their versions changed),
  * traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */
 int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
                        const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                        const ArtfCudaTraceOptions* options, float* hostHdr, ArtfCudaTraceStats* stats);
+
+/* ---- measurement ------------------------------------------------------------------------------- */
+
+/* The device's FP32 and FP64 fused multiply-add throughput, measured (flop/s, a multiply-add two):
+ * the denominators of the trace's roofline.  No reference counterpart.  stream: a cudaStream_t or NULL. */
+int artfCudaProbePeaks(void* stream, int device, double* fp32Flops, double* fp64Flops);
 
 #ifdef __cplusplus
 }

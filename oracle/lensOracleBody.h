@@ -49,13 +49,14 @@ static REAL FN(sineOf)(REAL turns) {
     return p * x2 * x + x;
 }
 
-/* lens.inc:89-96 lensRow: a map row at a turn, linear between two of its width (a power of two) columns. */
-static REAL FN(rowAt)(const float* map, int64_t count, int width, int32_t row, REAL turn) {
-    const REAL at = (turn - FLOOR(turn)) * (REAL)width;
-    const REAL column = FLOOR(at), part = at - column;
+/* lens.inc:89-96 lensRow: a row of a region (starting `at` floats into a buffer of `count`) at a turn,
+ * linear between two of its width (a power of two) columns. */
+static REAL FN(rowAt)(const float* buffer, int64_t count, int64_t at, int width, int32_t row, REAL turn) {
+    const REAL pos = (turn - FLOOR(turn)) * (REAL)width;
+    const REAL column = FLOOR(pos), part = pos - column;
     const int32_t base = (int32_t)((uint32_t)row * (uint32_t)width);
     const int32_t c0 = FN(toInt)(column) & (width - 1), c1 = (c0 + 1) & (width - 1);
-    const REAL a = FN(texel)(map, (int64_t)base + c0, count), b = FN(texel)(map, (int64_t)base + c1, count);
+    const REAL a = FN(texel)(buffer, at + base + c0, count), b = FN(texel)(buffer, at + base + c1, count);
     return a + (b - a) * part;
 }
 
@@ -133,9 +134,6 @@ static void FN(traceRay)(const FRAME* h, const float* map, const float* fluid, R
     const REAL inner = h->disc[0], thickness = h->disc[3], gain = h->look[0], doppler = h->look[1],
                discHeight = h->spin[2];
     const REAL rhoScale = (REAL)1 / ((REAL)1 - inner / h->disc[1]);
-    const float* rows = map + ORACLE_ROWS_AT;
-    const float* colors = map + ORACLE_COLORS_AT;
-    const int64_t rowsCount = mapCount - ORACLE_ROWS_AT, colorsCount = mapCount - ORACLE_COLORS_AT;
 
     REAL sum[3] = {0, 0, 0}, through = 1, away[3] = {0, 0, 0}, awayPsi = 0;
     int sky = 0, lit = 0, crossings = 0, steps = 0, kind = ORACLE_CAP;
@@ -209,25 +207,25 @@ static void FN(traceRay)(const FRAME* h, const float* map, const float* fluid, R
                     const REAL rowFloor = FN(minX)(FLOOR(rowPos), (REAL)(ORACLE_MAP_HEIGHT - 2));
                     const REAL rowPart = rowPos - rowFloor;
                     const int32_t row0 = FN(toInt)(rowFloor), row1 = row0 + 1;
-                    const REAL speed0 = FN(texel)(rows, (int64_t)row0 + row0, rowsCount);
-                    const REAL speed1 = FN(texel)(rows, (int64_t)row1 + row1, rowsCount);
+                    const REAL speed0 = FN(texel)(map, ORACLE_ROWS_AT + (int64_t)row0 + row0, mapCount);
+                    const REAL speed1 = FN(texel)(map, ORACLE_ROWS_AT + (int64_t)row1 + row1, mapCount);
                     const REAL turnK = turn + (inside ? rate * ds : 0);
-                    const REAL d0 = FN(rowAt)(map, mapCount, ORACLE_MAP_WIDTH, row0, turnK - speed0 * time);
-                    const REAL d1 = FN(rowAt)(map, mapCount, ORACLE_MAP_WIDTH, row1, turnK - speed1 * time);
+                    const REAL d0 = FN(rowAt)(map, mapCount, 0, ORACLE_MAP_WIDTH, row0, turnK - speed0 * time);
+                    const REAL d1 = FN(rowAt)(map, mapCount, 0, ORACLE_MAP_WIDTH, row1, turnK - speed1 * time);
                     REAL density = d0 + (d1 - d0) * rowPart;
                     /* 238-245: the fluid, each ring turned on since it was stepped */
                     const REAL fluidPos = (inside ? rhoK : 0) * (REAL)(ORACLE_FLUID_HEIGHT - 1);
                     const REAL fluidFloor = FN(minX)(FLOOR(fluidPos), (REAL)(ORACLE_FLUID_HEIGHT - 2));
                     const int32_t fluidRow = FN(toInt)(fluidFloor);
                     const REAL fluidTurn = turnK - speed0 * (REAL)(time - h->flow[0]);
-                    const REAL g0 = FN(rowAt)(fluid, fluidCount, ORACLE_FLUID_WIDTH, fluidRow, fluidTurn);
-                    const REAL g1 = FN(rowAt)(fluid, fluidCount, ORACLE_FLUID_WIDTH, fluidRow + 1, fluidTurn);
+                    const REAL g0 = FN(rowAt)(fluid, fluidCount, 0, ORACLE_FLUID_WIDTH, fluidRow, fluidTurn);
+                    const REAL g1 = FN(rowAt)(fluid, fluidCount, 0, ORACLE_FLUID_WIDTH, fluidRow + 1, fluidTurn);
                     const REAL gas = g0 + (g1 - g0) * (fluidPos - fluidFloor);
                     density = density * ((REAL)(1.f - .1f) + K(.1) * gas);
                     /* 247-250: dust */
                     const REAL dustPos = (inside ? rhoK : 0) * (REAL)(ORACLE_DUST_HEIGHT - 1);
                     const int32_t dustRow = FN(toInt)(FN(minX)(FLOOR(dustPos), (REAL)(ORACLE_DUST_HEIGHT - 1)));
-                    const REAL dusty = FN(rowAt)(map + ORACLE_DUST_AT, mapCount - ORACLE_DUST_AT, ORACLE_DUST_WIDTH,
+                    const REAL dusty = FN(rowAt)(map, mapCount, ORACLE_DUST_AT, ORACLE_DUST_WIDTH,
                                                  dustRow, turnK - speed0 * time);
                     const REAL litShare = (REAL)1 - K(.97) * dusty;
                     /* 252-258: height in the disc, opacity, emission */
@@ -243,8 +241,8 @@ static void FN(traceRay)(const FRAME* h, const float* map, const float* fluid, R
                 /* 262-279: the ring's heat and glow, and the Doppler and gravitational shift */
                 const REAL rhoSafe = FN(minX)(FN(maxX)(rhoCenter, 0), 1);
                 const int32_t rowIndex = FN(toInt)(rhoSafe * (REAL)(ORACLE_MAP_HEIGHT - 1));
-                REAL heat = FN(texel)(rows + 1, (int64_t)rowIndex + rowIndex, rowsCount - 1);
-                const REAL gives = FN(texel)(map + ORACLE_GLOW_AT, rowIndex, mapCount - ORACLE_GLOW_AT);
+                REAL heat = FN(texel)(map, ORACLE_ROWS_AT + 1 + (int64_t)rowIndex + rowIndex, mapCount);
+                const REAL gives = FN(texel)(map, ORACLE_GLOW_AT + (int64_t)rowIndex, mapCount);
                 REAL light = gain * glow * gives;
                 if (doppler != 0) {
                     const REAL safeU = FN(maxX)(uc, K(1e-4));
@@ -261,9 +259,9 @@ static void FN(traceRay)(const FRAME* h, const float* map, const float* fluid, R
                 /* 281-289: a black body's colour at that heat */
                 const REAL colorPos = FN(minX)(heat * (REAL)(ORACLE_COLORS / 2), (REAL)(ORACLE_COLORS - 1));
                 const int32_t color = FN(toInt)(colorPos);
-                const int64_t at = (int64_t)color + color + color;
-                const REAL rgb[3] = {FN(texel)(colors, at, colorsCount), FN(texel)(colors, at + 1, colorsCount),
-                                     FN(texel)(colors, at + 2, colorsCount)};
+                const int64_t at = ORACLE_COLORS_AT + (int64_t)color + color + color;
+                const REAL rgb[3] = {FN(texel)(map, at, mapCount), FN(texel)(map, at + 1, mapCount),
+                                     FN(texel)(map, at + 2, mapCount)};
                 for (int c = 0; c < 3; ++c) sum[c] = sum[c] + light * rgb[c];
                 through = clear;
                 if (light > 0 && !lit) {
@@ -313,10 +311,8 @@ static void FN(traceRay)(const FRAME* h, const float* map, const float* fluid, R
         const REAL heightPos = (dir[2] * K(.5) + K(.5)) * (REAL)(ORACLE_SKY_HEIGHT - 1);
         const REAL skyFloor = FN(minX)(FLOOR(heightPos), (REAL)(ORACLE_SKY_HEIGHT - 2));
         const int32_t skyRow = FN(toInt)(skyFloor);
-        const float* skyMap = map + ORACLE_SKY_AT;
-        const int64_t skyCount = mapCount - ORACLE_SKY_AT;
-        const REAL s0 = FN(rowAt)(skyMap, skyCount, ORACLE_SKY_WIDTH, skyRow, skyTurn);
-        const REAL s1 = FN(rowAt)(skyMap, skyCount, ORACLE_SKY_WIDTH, skyRow + 1, skyTurn);
+        const REAL s0 = FN(rowAt)(map, mapCount, ORACLE_SKY_AT, ORACLE_SKY_WIDTH, skyRow, skyTurn);
+        const REAL s1 = FN(rowAt)(map, mapCount, ORACLE_SKY_AT, ORACLE_SKY_WIDTH, skyRow + 1, skyTurn);
         const REAL dust = s0 + (s1 - s0) * (heightPos - skyFloor);
         rgb[0] = rgb[0] + dust * K(.92);
         rgb[1] = rgb[1] + dust * K(.86);

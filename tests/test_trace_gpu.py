@@ -1,0 +1,148 @@
+"""Parity of the CUDA traces through the C ABI, on a GB300.
+
+  exact  the reference's bits: against the golden fixtures (the reference's own outputs) and the oracle
+  fp32   FMA and fast reciprocals: pixel classes and radiance within the stated tolerances
+  fp64   plain double: against the oracle's double instantiation
+  mixed  FP32 with FP64 guards: endpoint error against the FP64 trace
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from artful_gb300 import capi, scenes
+from oracle import binding
+from tests import gpu_helpers as g
+
+pytestmark = pytest.mark.gpu
+
+WHOLE = [n for n, s in scenes.golden_scenes().items() if s.whole]
+
+
+def _scene_inputs(lib, name):
+    scene = scenes.golden_scenes()[name]
+    frame, frame64, clamped = scenes.frame(scene)
+    return scene, frame, frame64, scenes.synth_map(lib, clamped, scene.seed, scene.emissivity), scenes.unit_fluid()
+
+
+@pytest.mark.parametrize("name", list(scenes.golden_scenes()))
+def test_exact_rays_match_reference_bits(lib, ctx, golden, name):
+    _, arrays = golden
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, name)
+    g.set_inputs(lib, ctx, m, fluid)
+    rays = arrays[f"{name}_rays"]
+    rgb, _ = g.trace_rays(lib, ctx, frame, None, capi.EXACT, rays[:, 0], rays[:, 1], rays[:, 2])
+    want = arrays[f"{name}_rgb"]
+    assert np.array_equal(rgb.view(np.uint32), want.view(np.uint32)), np.argwhere(rgb != want)[:5]
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("name", WHOLE)
+def test_exact_frames_match_reference_bits(lib, ctx, golden, name, persistent):
+    meta, _ = golden
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, name)
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, stats = g.trace(lib, ctx, frame, None, capi.EXACT, persistent=persistent)
+    rgb = np.ascontiguousarray(hdr[..., :3])
+    assert hashlib.sha256(rgb.tobytes()).hexdigest() == meta["views"][name]["hdr_sha256"]
+    assert stats.rays == scene.width * scene.height * frame.size[2] ** 2
+
+
+def test_exact_jittered_1080p_rows_match_reference_bits(lib, ctx, golden):
+    meta, arrays = golden
+    scene = scenes.config2(4)
+    frame, frame64, clamped = scenes.frame(scene)
+    g.set_inputs(lib, ctx, scenes.synth_map(lib, clamped, scene.seed, scene.emissivity), scenes.unit_fluid())
+    hdr, stats = g.trace(lib, ctx, frame, None, capi.EXACT, jitter=4, seed=scene.jitter_seed)
+    assert stats.rays == 1920 * 1080 * 4
+    for i, y in enumerate(meta["c2_rows"]["rows"]):
+        assert np.array_equal(hdr[y, :, :3], arrays["c2_rows"][i])
+
+
+def test_exact_classes_and_ends_match_oracle(lib, ctx, golden):
+    _, arrays = golden
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, ends, stats = g.trace(lib, ctx, frame, None, capi.EXACT, ends=True)
+    ohdr, oends = binding.render32(frame, m, fluid, ends=True)
+    assert np.array_equal(hdr.view(np.uint32), ohdr.view(np.uint32))
+    for field in ("hitR", "hitPhi", "dir", "mino", "steps", "crossings", "kind"):
+        a, b = ends[field], oends[field]
+        same = (a == b) | (np.isnan(a) & np.isnan(b)) if a.dtype.kind == "f" else a == b
+        assert np.all(same), field
+    assert stats.steps == int(ends["steps"].astype(np.int64).sum())
+    assert stats.crossings == int(ends["crossings"].astype(np.int64).sum())
+    assert np.mean(g.classes_of(hdr[..., 3]) == arrays["c1_classes"]) == 1.0
+
+
+def _tolerance_report(hdr, want, bits_want):
+    ring = g.ring_mask(bits_want)
+    keep = ~ring
+    agree = np.mean(g.classes_of(hdr[..., 3])[keep] == g.classes_of(bits_want)[keep])
+    a = hdr[..., :3].astype(np.float64)
+    b = want[..., :3].astype(np.float64)
+    lum_a, lum_b = a.sum(-1), b.sum(-1)
+    rel = np.abs(lum_a - lum_b) / np.maximum(np.abs(lum_b), 1e-3)
+    return agree, rel[keep], ring.mean()
+
+
+def test_fast_fp32_within_tolerance(lib, ctx):
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, _ = g.trace(lib, ctx, frame, None, capi.FP32)
+    want = binding.render32(frame, m, fluid)
+    agree, rel, _ = _tolerance_report(hdr, want, want[..., 3])
+    assert agree >= 0.999
+    assert np.quantile(rel, 0.99) <= 1e-3
+    assert abs(hdr[..., :3].astype(np.float64).sum() / want[..., :3].astype(np.float64).sum() - 1) < 1e-3
+
+
+def test_fp64_matches_double_oracle(lib, ctx):
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_101x67")
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, ends, _ = g.trace(lib, ctx, frame, frame64, capi.FP64, ends=True)
+    want, oends = binding.render64(frame, frame64, m, fluid, ends=True)
+    agree, rel, _ = _tolerance_report(hdr, want.astype(np.float32), want[..., 3])
+    assert agree >= 0.999
+    assert np.quantile(rel, 0.99) <= 1e-5
+    same_steps = np.mean(ends["steps"] == oends["steps"])
+    assert same_steps >= 0.99
+
+
+def test_mixed_endpoints_against_fp64(lib, ctx):
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, ends, stats = g.trace(lib, ctx, frame, frame64, capi.MIXED, ends=True)
+    ref, rends, _ = g.trace(lib, ctx, frame, frame64, capi.FP64, ends=True)
+    agree, rel, _ = _tolerance_report(hdr, ref, ref[..., 3])
+    assert agree >= 0.999
+    assert np.quantile(rel, 0.99) <= 1e-3
+    assert 0 < stats.fp64Steps < stats.steps
+
+
+def test_host_path_equals_device_path(lib, ctx):
+    import ctypes as C
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_101x67")
+    out = np.zeros((scene.height, scene.width, 4), np.float32)
+    opts = capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 0)
+    capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), None, m.ctypes.data, 1, fluid.ctypes.data, 1,
+                                      C.byref(opts), out.ctypes.data, None))
+    g.set_inputs(lib, ctx, m, fluid)
+    hdr, _ = g.trace(lib, ctx, frame, None, capi.EXACT)
+    assert np.array_equal(out.view(np.uint32), hdr.view(np.uint32))
+
+
+def test_bad_options_are_refused(lib, ctx):
+    import ctypes as C
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_3x2")
+    g.set_inputs(lib, ctx, m, fluid)
+    import torch
+    hdr = torch.empty((2, 3, 4), device="cuda")
+    for opts in (capi.TraceOptions(7, 0, 0, 1.0, 0, 0, 0, 0), capi.TraceOptions(0, -1, 0, 1.0, 0, 0, 0, 0),
+                 capi.TraceOptions(0, 0, 0, 2.0, 0, 0, 0, 0)):
+        assert lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(opts), hdr.data_ptr(), None,
+                                     None) == capi_einval()
+
+
+def capi_einval():
+    return -1
