@@ -41,7 +41,35 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--quick", action="store_true", help="skip the slow side measurements")
+    p.add_argument("--profile", choices=["mixed", "fp64", "exact", "fp32"],
+                   help="trace one frame of that precision (after one untimed one) and exit: the case for ncu")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
     return p.parse_args()
+
+
+def profile_case(args):
+    """One warm-up and one traced frame of one precision at the given size, nothing else."""
+    from artful_gb300 import capi, scenes
+    import torch
+    lib = capi.load()
+    ctx = C.c_void_p()
+    capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
+    scene = scenes.config2(4)
+    scene.width, scene.height = args.width, args.height
+    frame, frame64, clamped = scenes.frame(scene)
+    map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
+    capi.check(lib.artfCudaSetFluid(ctx, scenes.unit_fluid().ctypes.data, 1))
+    hdr = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
+    o = capi.TraceOptions(capi.PRECISIONS[args.profile], 4, scene.jitter_seed, 1.0, 0.0, 0, 0, 0)
+    for _ in range(2):
+        s = capi.TraceStats()
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                                         hdr.data_ptr(), None, C.byref(s)))
+    print(json.dumps({"profile": args.profile, "width": scene.width, "height": scene.height, "ms": s.ms,
+                      "rays": s.rays, "steps": s.steps, "fp64Steps": s.fp64Steps, "flops": s.flops}))
+    lib.artfCudaDestroy(ctx)
 
 
 def dist_setup(args):
@@ -175,6 +203,9 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    if args.profile:
+        profile_case(args)
+        return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
