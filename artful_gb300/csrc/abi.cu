@@ -143,6 +143,9 @@ static int checkFrame(const ArtfCudaHoleFrame* f, const ArtfCudaTraceOptions* o)
     if (o->precision < ARTF_CUDA_EXACT || o->precision > ARTF_CUDA_MIXED)
         return fail(ARTF_CUDA_EINVAL, "unknown precision %d", o->precision);
     if (o->stepScale < 0.f || o->stepScale > 1.f) return fail(ARTF_CUDA_EINVAL, "stepScale out of [0, 1]");
+    if (o->guards > ARTF_CUDA_GUARD_ALL) return fail(ARTF_CUDA_EINVAL, "unknown guard bits %#x", o->guards);
+    if (o->fp64Batch < 0 || o->fp64Batch > 32) return fail(ARTF_CUDA_EINVAL, "fp64Batch out of 0..32");
+    if (o->horizonBand < 0.f || o->horizonBand > 1.f) return fail(ARTF_CUDA_EINVAL, "horizonBand out of [0, 1]");
     return ARTF_CUDA_OK;
 }
 
@@ -173,6 +176,10 @@ static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCuda
         stats->crossings = c[artf::CCrossings];
         stats->escapes = c[artf::CEscapes];
         stats->fp64Steps = precision == ARTF_CUDA_FP64 ? c[artf::CSteps] : c[artf::CFp64Steps];
+        stats->fp64Horizon = c[artf::CFp64Horizon];
+        stats->fp64Radial = c[artf::CFp64Radial];
+        stats->fp64Polar = c[artf::CFp64Polar];
+        stats->fp64Rounds = c[artf::CFp64Rounds];
         stats->flops = artfFlops(stats->rays, stats->steps, stats->crossings, stats->escapes, l.frame.spin[0] != 0.f,
                                  l.frame.look[1] != 0.f, l.frame.look[2] > 0.f);
         stats->ms = ms;
@@ -235,6 +242,8 @@ extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, 
     l.blockSize = options->blockSize;
     l.compactEvery = options->compactEvery;
     l.persistent = options->persistent;
+    l.guards = options->guards;
+    l.fp64Batch = options->fp64Batch;
     return runTrace(ctx, l, options->precision, stats);
 }
 

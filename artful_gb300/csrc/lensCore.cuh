@@ -173,42 +173,62 @@ template <typename R> ARTF_HD R dragAt(R a, R a2, R xiA, R x) {
 
 template <typename R> ARTF_HD R bendAt(const RayConst<R>& c, R x) { return x * (c.uA + x * (c.uB + x * c.uC)); }
 
-/* lens.inc:165-192: one Nystrom step of (u, n) and Simpson's rule for psi. */
-template <typename R> ARTF_HD void nystromStep(R a, const RayConst<R>& c, const RayState<R>& s, StepOut<R>& o) {
-    const R a2 = a * a, twoA2 = KF(2.) * a2;
+/* The step decouples: u'' depends on u alone and n'' on n alone (lens.inc:7-8), and psi' on u alone.
+ * So one Nystrom step is a radial sub-step of (u, w, psi) and a polar sub-step of (n, v), with the same
+ * operations either way; the mixed-precision trace runs each in the precision it needs. */
+
+/* lens.inc:165-192, the radial part: u, du/ds, and Simpson's rule for psi. */
+template <typename R>
+ARTF_HD void radialStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R& k1Out) {
+    const R a2 = a * a;
     const R step = c.step, step2 = step * step;
     const R half = step * KF(.5), eighth = step2 * KF(.125), halfSquare = step2 * KF(.5);
     const R sixthSquare = step2 * R(1.f / 6.f), sixth = step * R(1.f / 6.f);
     const R k1 = bendAt(c, s.u);
-    const R c1 = c.big + twoA2 * (s.n[2] * s.n[2]);
-    R a1[3] = {R(0) - c1 * s.n[0], R(0) - c1 * s.n[1], a2 * s.n[2] - c1 * s.n[2]};
     const R midU = s.u + half * s.w + eighth * k1;
+    const R k2 = bendAt(c, midU);
+    const R endU = s.u + step * s.w + halfSquare * k2;
+    const R k3 = bendAt(c, endU);
+    next.u = s.u + step * s.w + sixthSquare * (k1 + (k2 + k2));
+    next.w = s.w + sixth * (k1 + k3 + KF(4.) * k2);
+    if (a != R(0)) {
+        next.drag = dragAt(a, a2, c.xiA, next.u);
+        next.psi = s.psi + sixth * (s.drag + next.drag + KF(4.) * dragAt(a, a2, c.xiA, midU));
+    } else {
+        next.drag = R(0);
+        next.psi = R(0);
+    }
+    k1Out = k1;
+}
+
+/* lens.inc:165-192, the polar part: n on the sphere and dn/ds. */
+template <typename R>
+ARTF_HD void polarStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R* a1Out) {
+    const R a2 = a * a, twoA2 = KF(2.) * a2;
+    const R step = c.step, step2 = step * step;
+    const R half = step * KF(.5), eighth = step2 * KF(.125), halfSquare = step2 * KF(.5);
+    const R sixthSquare = step2 * R(1.f / 6.f), sixth = step * R(1.f / 6.f);
+    const R c1 = c.big + twoA2 * (s.n[2] * s.n[2]);
+    const R a1[3] = {R(0) - c1 * s.n[0], R(0) - c1 * s.n[1], a2 * s.n[2] - c1 * s.n[2]};
     R midN[3];
     for (int k = 0; k < 3; ++k) midN[k] = s.n[k] + half * s.v[k] + eighth * a1[k];
-    const R k2 = bendAt(c, midU);
     const R c2 = c.big + twoA2 * (midN[2] * midN[2]);
     const R a2s[3] = {R(0) - c2 * midN[0], R(0) - c2 * midN[1], a2 * midN[2] - c2 * midN[2]};
-    const R endU = s.u + step * s.w + halfSquare * k2;
     R endN[3];
     for (int k = 0; k < 3; ++k) endN[k] = s.n[k] + step * s.v[k] + halfSquare * a2s[k];
-    const R k3 = bendAt(c, endU);
     const R c3 = c.big + twoA2 * (endN[2] * endN[2]);
     const R a3[3] = {R(0) - c3 * endN[0], R(0) - c3 * endN[1], a2 * endN[2] - c3 * endN[2]};
-    o.next.u = s.u + step * s.w + sixthSquare * (k1 + (k2 + k2));
-    o.next.w = s.w + sixth * (k1 + k3 + KF(4.) * k2);
     for (int k = 0; k < 3; ++k) {
-        o.next.n[k] = s.n[k] + step * s.v[k] + sixthSquare * (a1[k] + (a2s[k] + a2s[k]));
-        o.next.v[k] = s.v[k] + sixth * (a1[k] + a3[k] + KF(4.) * a2s[k]);
+        next.n[k] = s.n[k] + step * s.v[k] + sixthSquare * (a1[k] + (a2s[k] + a2s[k]));
+        next.v[k] = s.v[k] + sixth * (a1[k] + a3[k] + KF(4.) * a2s[k]);
+        a1Out[k] = a1[k];
     }
-    if (a != R(0)) {
-        o.next.drag = dragAt(a, a2, c.xiA, o.next.u);
-        o.next.psi = s.psi + sixth * (s.drag + o.next.drag + KF(4.) * dragAt(a, a2, c.xiA, midU));
-    } else {
-        o.next.drag = R(0);
-        o.next.psi = R(0);
-    }
-    o.k1 = k1;
-    for (int k = 0; k < 3; ++k) o.a1[k] = a1[k];
+}
+
+/* lens.inc:165-192: one Nystrom step of (u, n) and Simpson's rule for psi. */
+template <typename R> ARTF_HD void nystromStep(R a, const RayConst<R>& c, const RayState<R>& s, StepOut<R>& o) {
+    radialStep(a, c, s, o.next, o.k1);
+    polarStep(a, c, s, o.next, o.a1);
 }
 
 /* A disc crossing inside one step: the ray's state at the plane (lens.inc:197-208, second-order Taylor

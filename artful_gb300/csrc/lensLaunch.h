@@ -10,7 +10,10 @@
 namespace artf {
 
 /* Device counters a trace adds to (unsigned 64-bit each). */
-enum Counter { CRays, CSteps, CCrossings, CEscapes, CFp64Steps, CQueue, CStatus, CCount };
+enum Counter {
+    CRays, CSteps, CCrossings, CEscapes, CFp64Steps, CQueue, CStatus,
+    CFp64Horizon, CFp64Radial, CFp64Polar, CFp64Rounds, CCount
+};
 
 struct TraceLaunch {
     ArtfCudaHoleFrame frame;      /* the FP32 frame (sample positions always come from it) */
@@ -27,6 +30,8 @@ struct TraceLaunch {
     int blockSize;
     int compactEvery;
     int persistent;
+    uint32_t guards;
+    int fp64Batch;
     int smCount;
     cudaStream_t stream;
     /* a list of rays in place of a frame's pixels (rayCount > 0) */

@@ -1,16 +1,28 @@
 /* artful_cuda — the mixed-precision trace: FP32 for the bulk of each geodesic, FP64 only where
  * stability needs it.
  *
- *   - the constants of motion (E, xi = L_z / E, Carter's eta, K) and the first state come from the ray
- *     at the eye in FP64, from the frame computed in double;
- *   - a step runs in FP64 when the ray is within a band of the outer horizon (u > band * 0.995/r+),
- *     where Delta / r^2 in the frame-drag rate loses most of its bits to cancellation, or when the FP32
- *     step brought a turning point: the radial (du/ds changes sign) or the polar one (the axis part of
- *     dn/ds changes sign);
- *   - psi, the frame-drag angle, is summed with a compensated (two-sum) accumulator, and the Mino time
- *     of the endpoint is formed in FP64 from the step count, so that neither drifts over 192 steps.
- * The disc and sky shading stay in FP32.  Built with the fast FP32 flags of lensFast.cu; double
- * arithmetic is IEEE throughout. */
+ *   MOTION   the constants of motion (E, xi = L_z / E, Carter's eta, K) and the first state come from
+ *            the ray at the eye in FP64, from the frame computed in double;
+ *   HORIZON  within a band of the outer horizon (u > band * 0.995 / r+) the radial sub-step of
+ *            (u, du/ds, psi) runs in FP64: Delta / r^2 in the frame-drag rate loses most of its bits to
+ *            cancellation there;
+ *   RADIAL   the step in which du/ds changes sign (the radial potential's zero) has its radial
+ *            sub-step in FP64;
+ *   POLAR    the step in which the axis part of dn/ds changes sign (the polar potential's zero) has
+ *            its polar sub-step of (n, dn/ds) in FP64;
+ *   PSI      psi, the frame-drag angle, is summed with a compensated (two-sum) accumulator, and the
+ *            endpoint's Mino time is formed in FP64 from the step count: neither drifts over 192 steps.
+ * The radial and polar sub-steps are independent (u'' depends on u alone, n'' on n alone), so a guard
+ * costs FP64 only for the part that needs it.  The disc and sky shading stay in FP32.  Built with the
+ * fast FP32 flags; double arithmetic is IEEE throughout.
+ *
+ * Scheduling (traceMixedQueue): the GB300's FP64 pipe is 1/72 of its FP32 pipe, and a warp pays for an
+ * FP64 instruction whatever number of its lanes take part.  So FP64 work runs in warp-wide rounds:
+ * lanes that need an FP64 sub-step (or a new ray's FP64 set-up) wait, keeping their FP32 results,
+ * while the others keep stepping in FP32; a round runs when `batch` lanes wait, when no lane can move
+ * without one, or after a bounded wait.  Pixels come from a device queue, a lane at a time, by warp
+ * ballot and shuffle.  Every lane computes exactly what the per-ray path (traceRayMixed) computes, in
+ * the same order: the schedule changes when, never what. */
 #include "lensKernel.cuh"
 
 namespace artf {
@@ -32,155 +44,335 @@ struct MixedParams {
     int rays;
     float share;
     int tilesX, tiles;
-    float uGuard;  /* FP64 steps above this u */
+    float uGuard;     /* the horizon band: radial FP64 sub-steps above this u */
+    uint32_t guards;  /* ARTF_CUDA_GUARD_* */
+    int batch;        /* lanes waiting before a warp runs an FP64 round */
+    int maxWait;      /* iterations a lane waits at most */
 };
 
-template <typename A, typename B> __device__ __forceinline__ void convertState(const RayState<A>& s, RayState<B>& o) {
-    o.u = B(s.u), o.w = B(s.w), o.psi = B(s.psi), o.drag = B(s.drag);
-    for (int k = 0; k < 3; ++k) o.n[k] = B(s.n[k]), o.v[k] = B(s.v[k]);
+/* One ray's state between steps. */
+struct MixedRay {
+    RayConst<float> c;
+    double big, step, uA, uB, uC, xiA; /* the FP64 coefficients the guarded sub-steps use */
+    RayState<float> s;                 /* s.psi stays 0: a step returns psi's increment */
+    float psiHi, psiLo, through, sum[3], hitR, hitPhi;
+    int i;
+    unsigned crossings, wide;
+    bool lit;
+};
+
+__device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
+    RayConst<double> c;
+    c.big = r.big, c.step = r.step, c.uA = r.uA, c.uB = r.uB, c.uC = r.uC, c.xiA = r.xiA;
+    c.invEnergy = c.xi = c.moved = c.time = 0.0; /* (not read by the sub-steps) */
+    return c;
 }
 
-__device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, float nx, float ny, float time, float* sum,
-                                                  ArtfCudaRayEnd* end, Tally& t, unsigned& wideSteps) {
-    const Frame<float>& f = p.f;
-    /* the ray at the eye and its constants of motion in FP64 */
-    RayConst<double> cd;
-    RayState<double> sd;
-    rayStart(p.d, (double)nx, (double)ny, (double)time, (double)p.stepScale, cd, sd);
-    const double ad = p.d.a, a2d = ad * ad;
-    if (ad != 0.0) sd.drag = dragAt(ad, a2d, cd.xiA, sd.u);
-    RayConst<float> c;
-    c.invEnergy = (float)cd.invEnergy, c.xi = (float)cd.xi, c.moved = (float)cd.moved, c.big = (float)cd.big;
-    c.step = (float)cd.step, c.uA = (float)cd.uA, c.uB = (float)cd.uB, c.uC = (float)cd.uC, c.xiA = (float)cd.xiA;
-    c.time = time;
-    RayState<float> s;
-    convertState(sd, s);
-    s.psi = 0.f; /* the steps return psi's increment; the sum is kept apart, compensated */
-    const float a = f.a;
-    const float rhoScale = 1.f / (1.f - f.inner / f.outer);
-
-    float psiHi = 0.f, psiLo = 0.f;
-    float raySum[3] = {0.f, 0.f, 0.f}, through = 1.f;
-    unsigned kind = ARTF_CUDA_END_CAP, crossings = 0, wide = 0;
-    bool lit = false;
-    float hitR = NAN, hitPhi = NAN, dir[3] = {0.f, 0.f, 0.f};
-    double mino = (double)p.maxSteps * cd.step;
-    int i = 0;
-    for (; i < p.maxSteps; ++i) {
-        StepOut<float> o;
-        bool inFp64 = s.u > p.uGuard;
-        if (!inFp64) {
-            nystromStep(a, c, s, o);
-            /* a turning point inside the step: take it again in FP64 */
-            inFp64 = (s.w > 0.f) != (o.next.w > 0.f) || (s.v[2] > 0.f) != (o.next.v[2] > 0.f);
-        }
-        if (inFp64) {
-            RayState<double> wideState;
-            convertState(s, wideState);
-            StepOut<double> od;
-            nystromStep(ad, cd, wideState, od);
-            convertState(od.next, o.next);
-            o.k1 = (float)od.k1;
-            for (int k = 0; k < 3; ++k) o.a1[k] = (float)od.a1[k];
-            ++wide;
-        }
-        const float increment = o.next.psi;
-
-        Crossing<float> x;
-        if (crossingOf(f, rhoScale, c, s, o, x)) {
-            x.psiC = psiHi + (psiLo + x.part * increment);
-            ++crossings;
-            float turn;
-            const float light = shadeCrossing(f, rhoScale, p.map, p.fluid, c, x, through, raySum, &turn);
-            if (light > 0.f && !lit) {
-                lit = true;
-                hitR = 1.f / x.uc;
-                hitPhi = turn - floorf(turn);
-            }
-        }
-        if (0.f > o.next.u) {
-            const float part = s.u / (s.u - o.next.u);
-            float away[3];
-            for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
-            const float awayPsi = psiHi + (psiLo + part * increment);
-            skyDirection(away, awayPsi, dir);
-            if (f.stars > 0.f) shadeSky(f, p.map, c, dir, through, raySum);
-            kind = ARTF_CUDA_END_SKY;
-            mino = ((double)i + (double)part) * cd.step;
-            ++i;
-            break;
-        }
-        if (o.next.u > f.uHorizon) { kind = ARTF_CUDA_END_HORIZON; mino = (double)(i + 1) * cd.step; ++i; break; }
-        if (!(through > .004f)) { kind = ARTF_CUDA_END_OPAQUE; mino = (double)(i + 1) * cd.step; ++i; break; }
-        /* psi += increment, with the rounding error carried (Knuth's two-sum) */
-        const float sumHi = psiHi + increment, back = sumHi - psiHi;
-        psiLo += (psiHi - (sumHi - back)) + (increment - back);
-        psiHi = sumHi;
-        s = o.next;
-        s.psi = 0.f;
+/* A ray's start: its constants of motion and first state, in FP64 under the MOTION guard. */
+__device__ __forceinline__ void mixedStart(const MixedParams& p, float nx, float ny, float time, MixedRay& r) {
+    if (p.guards & ARTF_CUDA_GUARD_MOTION) {
+        RayConst<double> cd;
+        RayState<double> sd;
+        rayStart(p.d, (double)nx, (double)ny, (double)time, (double)p.stepScale, cd, sd);
+        r.c.invEnergy = (float)cd.invEnergy, r.c.xi = (float)cd.xi, r.c.moved = (float)cd.moved;
+        r.c.big = (float)cd.big, r.c.step = (float)cd.step, r.c.uA = (float)cd.uA, r.c.uB = (float)cd.uB;
+        r.c.uC = (float)cd.uC, r.c.xiA = (float)cd.xiA;
+        r.big = cd.big, r.step = cd.step, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
+        r.s.u = (float)sd.u, r.s.w = (float)sd.w;
+        for (int k = 0; k < 3; ++k) r.s.n[k] = (float)sd.n[k], r.s.v[k] = (float)sd.v[k];
+    } else {
+        rayStart(p.f, nx, ny, time, p.stepScale, r.c, r.s);
+        r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
     }
-    for (int k = 0; k < 3; ++k) sum[k] = sum[k] + raySum[k];
-    if (lit) kind |= ARTF_CUDA_END_LIT;
+    r.c.time = time;
+    r.s.psi = 0.f;
+    r.s.drag = p.f.a != 0.f ? dragAt(p.f.a, p.f.a * p.f.a, r.c.xiA, r.s.u) : 0.f;
+    r.psiHi = r.psiLo = 0.f;
+    r.through = 1.f;
+    r.sum[0] = r.sum[1] = r.sum[2] = 0.f;
+    r.hitR = r.hitPhi = NAN;
+    r.i = 0;
+    r.crossings = r.wide = 0;
+    r.lit = false;
+}
+
+/* Which sub-steps of this FP32 step must run again in FP64. */
+__device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedRay& r, const StepOut<float>& o,
+                                           bool& radial, bool& polar, unsigned& reason) {
+    const bool band = (p.guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > p.uGuard;
+    const bool turnR = (p.guards & ARTF_CUDA_GUARD_RADIAL) && ((r.s.w > 0.f) != (o.next.w > 0.f));
+    polar = (p.guards & ARTF_CUDA_GUARD_POLAR) && ((r.s.v[2] > 0.f) != (o.next.v[2] > 0.f));
+    radial = band || turnR;
+    reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
+}
+
+__device__ __forceinline__ void radialWide(const MixedParams& p, const MixedRay& r, StepOut<float>& o) {
+    RayState<double> s, next;
+    s.u = r.s.u, s.w = r.s.w, s.psi = 0.0, s.drag = r.s.drag;
+    double k1;
+    radialStep(p.d.a, wideConst(r), s, next, k1);
+    o.next.u = (float)next.u, o.next.w = (float)next.w, o.next.psi = (float)next.psi, o.next.drag = (float)next.drag;
+    o.k1 = (float)k1;
+}
+
+__device__ __forceinline__ void polarWide(const MixedParams& p, const MixedRay& r, StepOut<float>& o) {
+    RayState<double> s, next;
+    for (int k = 0; k < 3; ++k) s.n[k] = r.s.n[k], s.v[k] = r.s.v[k];
+    double a1[3];
+    polarStep(p.d.a, wideConst(r), s, next, a1);
+    for (int k = 0; k < 3; ++k) o.next.n[k] = (float)next.n[k], o.next.v[k] = (float)next.v[k], o.a1[k] = (float)a1[k];
+}
+
+/* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
+ * (ARTF_CUDA_END_*) + 1, or 0 when the ray goes on. */
+__device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, float rhoScale, MixedRay& r,
+                                                 const StepOut<float>& o) {
+    const Frame<float>& f = p.f;
+    const bool compensated = p.guards & ARTF_CUDA_GUARD_PSI;
+    const float increment = o.next.psi;
+    Crossing<float> x;
+    if (crossingOf(f, rhoScale, r.c, r.s, o, x)) {
+        x.psiC = compensated ? r.psiHi + (r.psiLo + x.part * increment) : r.psiHi + x.part * increment;
+        ++r.crossings;
+        float turn;
+        const float light = shadeCrossing(f, rhoScale, p.map, p.fluid, r.c, x, r.through, r.sum, &turn);
+        if (light > 0.f && !r.lit) {
+            r.lit = true;
+            r.hitR = 1.f / x.uc;
+            r.hitPhi = turn - floorf(turn);
+        }
+    }
+    const int i = r.i++;
+    if (0.f > o.next.u) {
+        const float part = r.s.u / (r.s.u - o.next.u);
+        float away[3], dir[3];
+        for (int k = 0; k < 3; ++k) away[k] = r.s.n[k] + part * (o.next.n[k] - r.s.n[k]);
+        const float awayPsi = compensated ? r.psiHi + (r.psiLo + part * increment) : r.psiHi + part * increment;
+        skyDirection(away, awayPsi, dir);
+        if (f.stars > 0.f) shadeSky(f, p.map, r.c, dir, r.through, r.sum);
+        /* (the escape's direction and moment travel in the slots the ray no longer needs) */
+        r.s.n[0] = dir[0], r.s.n[1] = dir[1], r.s.n[2] = dir[2];
+        r.s.w = part;
+        return ARTF_CUDA_END_SKY + 1;
+    }
+    if (o.next.u > f.uHorizon) return ARTF_CUDA_END_HORIZON + 1;
+    if (!(r.through > .004f)) return ARTF_CUDA_END_OPAQUE + 1;
+    if (compensated) {
+        const float sumHi = r.psiHi + increment, back = sumHi - r.psiHi;
+        r.psiLo += (r.psiHi - (sumHi - back)) + (increment - back);
+        r.psiHi = sumHi;
+    } else {
+        r.psiHi += increment;
+    }
+    r.s = o.next;
+    r.s.psi = 0.f;
+    (void)i;
+    return r.i >= p.maxSteps ? ARTF_CUDA_END_CAP + 1 : 0u;
+}
+
+/* The end record of a finished ray, and its tallies. */
+__device__ __forceinline__ unsigned mixedFinish(const MixedParams& p, const MixedRay& r, unsigned ended,
+                                                ArtfCudaRayEnd* end, Tally& t) {
+    unsigned kind = ended - 1;
+    if (r.lit) kind |= ARTF_CUDA_END_LIT;
     t.rays += 1;
-    t.steps += (unsigned)i;
-    t.crossings += crossings;
-    t.escapes += (kind & 15u) == ARTF_CUDA_END_SKY;
-    wideSteps += wide;
+    t.steps += (unsigned)r.i;
+    t.crossings += r.crossings;
+    const bool sky = (kind & 15u) == ARTF_CUDA_END_SKY;
+    t.escapes += sky;
     if (end) {
         ArtfCudaRayEnd e;
-        e.hitR = hitR;
-        e.hitPhi = hitPhi;
-        for (int k = 0; k < 3; ++k) e.dir[k] = dir[k];
-        e.mino = (float)mino;
-        e.steps = (uint16_t)i;
-        e.crossings = (uint8_t)(crossings > 255u ? 255u : crossings);
+        e.hitR = r.hitR;
+        e.hitPhi = r.hitPhi;
+        for (int k = 0; k < 3; ++k) e.dir[k] = sky ? r.s.n[k] : 0.f;
+        e.mino = (float)(sky ? ((double)(r.i - 1) + (double)r.s.w) * r.step : (double)r.i * r.step);
+        e.steps = (uint16_t)r.i;
+        e.crossings = (uint8_t)(r.crossings > 255u ? 255u : r.crossings);
         e.kind = (uint8_t)kind;
-        e.fp64Steps = (uint16_t)wide;
+        e.fp64Steps = (uint16_t)r.wide;
         e.reserved = 0;
         *end = e;
     }
     return kind;
 }
 
-__global__ void __launch_bounds__(128) traceMixedTiles(const MixedParams p) {
+struct Reasons {
+    unsigned wide = 0, horizon = 0, radial = 0, polar = 0, rounds = 0;
+};
+
+__device__ __forceinline__ void countReason(unsigned reason, Reasons& n) {
+    n.wide += 1;
+    n.horizon += reason & 1u;
+    n.radial += (reason >> 1) & 1u;
+    n.polar += (reason >> 2) & 1u;
+}
+
+/* The per-ray path: one ray from start to end, each step's FP64 sub-steps at once. */
+__device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, float nx, float ny, float time, float* sum,
+                                                  ArtfCudaRayEnd* end, Tally& t, Reasons& n) {
+    MixedRay r;
+    mixedStart(p, nx, ny, time, r);
+    const float rhoScale = 1.f / (1.f - p.f.inner / p.f.outer);
+    unsigned ended = 0;
+    while (!ended) {
+        StepOut<float> o;
+        nystromStep(p.f.a, r.c, r.s, o);
+        bool radial, polar;
+        unsigned reason;
+        mixedNeeds(p, r, o, radial, polar, reason);
+        if (radial) radialWide(p, r, o);
+        if (polar) polarWide(p, r, o);
+        if (radial || polar) {
+            ++r.wide;
+            countReason(reason, n);
+        }
+        ended = mixedAdvance(p, rhoScale, r, o);
+    }
+    for (int k = 0; k < 3; ++k) sum[k] = sum[k] + r.sum[k];
+    return mixedFinish(p, r, ended, end, t);
+}
+
+__device__ __forceinline__ void flushReasons(const Reasons& n, unsigned long long* counters) {
+    const unsigned wide = __reduce_add_sync(0xFFFFFFFFu, n.wide);
+    const unsigned horizon = __reduce_add_sync(0xFFFFFFFFu, n.horizon);
+    const unsigned radial = __reduce_add_sync(0xFFFFFFFFu, n.radial);
+    const unsigned polar = __reduce_add_sync(0xFFFFFFFFu, n.polar);
+    const unsigned rounds = __reduce_add_sync(0xFFFFFFFFu, n.rounds);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counters + CFp64Steps, (unsigned long long)wide);
+        atomicAdd(counters + CFp64Horizon, (unsigned long long)horizon);
+        atomicAdd(counters + CFp64Radial, (unsigned long long)radial);
+        atomicAdd(counters + CFp64Polar, (unsigned long long)polar);
+        atomicAdd(counters + CFp64Rounds, (unsigned long long)rounds);
+    }
+}
+
+/* Pixel unit u (8 x 4 tiles in row-major tile order) to (x, y). */
+__device__ __forceinline__ void unitPixel(const MixedParams& p, int u, int& x, int& y) {
+    const int tile = u >> 5, within = u & 31;
+    x = (tile % p.tilesX) * 8 + (within & 7);
+    y = (tile / p.tilesX) * 4 + (within >> 3);
+}
+
+/* The warp-scheduled trace (see the file's head). */
+__global__ void __launch_bounds__(128) traceMixedQueue(const MixedParams p) {
+    const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
-    const int tile = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const unsigned below = (1u << lane) - 1u;
+    const int units = p.tiles * 32;
+    const float rhoScale = 1.f / (1.f - p.f.inner / p.f.outer);
     Tally t;
-    unsigned wideSteps = 0;
-    if (tile < p.tiles) {
-        const int32_t x = (tile % p.tilesX) * 8 + (lane & 7), y = (tile / p.tilesX) * 4 + (lane >> 3);
-        if (x < p.f.width && y < p.f.height) {
-            const size_t pixel = (size_t)y * (size_t)p.f.width + (size_t)x;
-            float sum[3] = {0.f, 0.f, 0.f};
-            unsigned bits = 0;
-            for (int k = 0; k < p.rays; ++k) {
+    Reasons n;
+    int unit = -1, x = 0, y = 0, k = 0;
+    bool exhausted = false, live = false, haveStep = false, waitR = false, waitP = false;
+    unsigned reason = 0, bits = 0;
+    float pixel[3] = {0.f, 0.f, 0.f};
+    MixedRay r;
+    StepOut<float> o;
+    int sinceStart = 0, sinceRadial = 0, sincePolar = 0;
+    /* Every iteration either advances some lane's ray by a step, starts rays, or ends the loop: the queue
+     * is finite and a ray ends within maxSteps steps, so the loop ends. */
+    for (;;) {
+        /* (1) refill, batched: the set-up of a ray is FP64 work */
+        const unsigned idle = __ballot_sync(full, !live && !exhausted);
+        const unsigned liveMask = __ballot_sync(full, live);
+        if (idle && (__popc(idle) >= p.batch || liveMask == 0 || sinceStart >= p.maxWait)) {
+            sinceStart = 0;
+            const bool needPixel = !live && !exhausted && (unit < 0 || k >= p.rays);
+            const unsigned fetch = __ballot_sync(full, needPixel);
+            if (fetch) {
+                const int leader = __ffs(fetch) - 1;
+                int base = 0;
+                if (lane == leader) base = (int)atomicAdd(p.counters + CQueue, (unsigned long long)__popc(fetch));
+                base = __shfl_sync(full, base, leader);
+                if (needPixel) {
+                    unit = base + __popc(fetch & below);
+                    k = 0, bits = 0;
+                    pixel[0] = pixel[1] = pixel[2] = 0.f;
+                    if (unit >= units) {
+                        exhausted = true;
+                        unit = -1;
+                    } else {
+                        unitPixel(p, unit, x, y);
+                        if (x >= p.f.width || y >= p.f.height) k = p.rays; /* (off the image: fetch again) */
+                    }
+                }
+            }
+            if (!live && unit >= 0 && k < p.rays) {
                 float nx, ny, moment;
                 samplePosition(p.h, p.jitter, p.seed, x, y, k, &nx, &ny, &moment);
-                const float time = p.h.disc[2] + p.h.spin[3] * moment;
-                ArtfCudaRayEnd* end = p.ends ? p.ends + pixel * (size_t)p.rays + (size_t)k : nullptr;
-                bits |= classBits(traceRayMixed(p, nx, ny, time, sum, end, t, wideSteps));
+                mixedStart(p, nx, ny, p.h.disc[2] + p.h.spin[3] * moment, r);
+                live = true;
             }
-            p.hdr[pixel] = make_float4(sum[0] * p.share, sum[1] * p.share, sum[2] * p.share, (float)bits);
+        } else if (idle) {
+            ++sinceStart;
+        }
+        if (__all_sync(full, exhausted && !live)) break;
+
+        /* (2) FP32 steps for the lanes not waiting on FP64 */
+        if (live && !haveStep) {
+            nystromStep(p.f.a, r.c, r.s, o);
+            mixedNeeds(p, r, o, waitR, waitP, reason);
+            haveStep = true;
+            if (waitR || waitP) {
+                ++r.wide;
+                countReason(reason, n);
+            }
+        }
+        /* (3) FP64 rounds, when enough lanes wait or nothing else can move */
+        const unsigned ready = __ballot_sync(full, haveStep && !waitR && !waitP);
+        const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
+        if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
+            if (waitR) {
+                radialWide(p, r, o);
+                waitR = false;
+            }
+            sinceRadial = 0;
+            n.rounds += lane == 0;
+        } else if (needR) {
+            ++sinceRadial;
+        }
+        if (needP && (__popc(needP) >= p.batch || ready == 0 || sincePolar >= p.maxWait)) {
+            if (waitP) {
+                polarWide(p, r, o);
+                waitP = false;
+            }
+            sincePolar = 0;
+            n.rounds += lane == 0;
+        } else if (needP) {
+            ++sincePolar;
+        }
+        /* (4) commit the steps that are complete */
+        if (haveStep && !waitR && !waitP) {
+            haveStep = false;
+            const unsigned ended = mixedAdvance(p, rhoScale, r, o);
+            if (ended) {
+                const size_t index = (size_t)y * (size_t)p.f.width + (size_t)x;
+                ArtfCudaRayEnd* end = p.ends ? p.ends + index * (size_t)p.rays + (size_t)k : nullptr;
+                bits |= classBits(mixedFinish(p, r, ended, end, t));
+                for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
+                live = false;
+                if (++k == p.rays)
+                    p.hdr[index] = make_float4(pixel[0] * p.share, pixel[1] * p.share, pixel[2] * p.share, (float)bits);
+            }
         }
     }
     flushTally(t, p.counters);
-    const unsigned wide = __reduce_add_sync(0xFFFFFFFFu, wideSteps);
-    if (lane == 0) atomicAdd(p.counters + CFp64Steps, (unsigned long long)wide);
+    flushReasons(n, p.counters);
 }
 
-__global__ void __launch_bounds__(128) traceMixedList(const MixedParams p, const int n, const float* nx,
+__global__ void __launch_bounds__(128) traceMixedList(const MixedParams p, const int count, const float* nx,
                                                       const float* ny, const float* time, float* rgb) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     Tally t;
-    unsigned wideSteps = 0;
-    if (i < n) {
+    Reasons n;
+    if (i < count) {
         float sum[3] = {0.f, 0.f, 0.f};
-        traceRayMixed(p, nx[i], ny[i], time[i], sum, p.ends ? p.ends + i : nullptr, t, wideSteps);
+        traceRayMixed(p, nx[i], ny[i], time[i], sum, p.ends ? p.ends + i : nullptr, t, n);
         for (int k = 0; k < 3; ++k) rgb[3 * i + k] = sum[k];
     }
     flushTally(t, p.counters);
-    const unsigned wide = __reduce_add_sync(0xFFFFFFFFu, wideSteps);
-    if ((threadIdx.x & 31) == 0) atomicAdd(p.counters + CFp64Steps, (unsigned long long)wide);
+    flushReasons(n, p.counters);
 }
 
 }  // namespace
@@ -204,14 +396,21 @@ cudaError_t launchMixed(const TraceLaunch& l) {
     p.tilesX = ((int)l.frame.size[0] + 7) / 8;
     p.tiles = p.tilesX * (((int)l.frame.size[1] + 3) / 4);
     p.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .5f) * l.frame64.spin[1]);
+    p.guards = l.guards ? l.guards : ARTF_CUDA_GUARD_ALL;
+    p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 16;
+    p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
     const int block = 128;
     if (l.rayCount > 0) {
         traceMixedList<<<(l.rayCount + block - 1) / block, block, 0, l.stream>>>(p, l.rayCount, l.rayX, l.rayY,
                                                                                  l.rayTime, l.rayRgb);
         return cudaGetLastError();
     }
-    const int grid = (p.tiles * 32 + block - 1) / block;
-    traceMixedTiles<<<grid, block, 0, l.stream>>>(p);
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueue, block, 0);
+    int grid = (perSm > 0 ? perSm : 1) * l.smCount;
+    const int needed = (p.tiles * 32 + block - 1) / block;
+    if (grid > needed) grid = needed;
+    traceMixedQueue<<<grid, block, 0, l.stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -45,7 +45,72 @@ def parse():
                    help="trace one frame of that precision (after one untimed one) and exit: the case for ncu")
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--sweep", action="store_true",
+                   help="time the mixed trace's guard, band and batch variants, each with its endpoint error")
     return p.parse_args()
+
+
+def sweep(args):
+    """One JSON line per variant of the mixed trace: time, FP64 work by reason, endpoint error against
+    FP64 at the same step and at half step."""
+    import torch
+    from artful_gb300 import capi, scenes
+    from oracle.binding import END_DTYPE
+    lib = capi.load()
+    ctx = C.c_void_p()
+    capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
+    scene = scenes.config2(4)
+    frame, frame64, clamped = scenes.frame(scene)
+    map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
+    capi.check(lib.artfCudaSetFluid(ctx, scenes.unit_fluid().ctypes.data, 1))
+    w, h, rays = scene.width, scene.height, 4
+    hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    ends = torch.empty((w * h * rays * 32,), dtype=torch.uint8, device="cuda")
+
+    def run(opts, with_ends=False, steps=0):
+        s = capi.TraceStats()
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts),
+                                         hdr.data_ptr(), ends.data_ptr() if with_ends else None, C.byref(s)))
+        times = []
+        for _ in range(steps):
+            t = capi.TraceStats()
+            capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts),
+                                             hdr.data_ptr(), None, C.byref(t)))
+            times.append(t.ms)
+        e = np.frombuffer(ends.cpu().numpy().tobytes(), END_DTYPE).copy() if with_ends else None
+        return s, (statistics.median(times) if times else s.ms), e, hdr.cpu().numpy().copy()
+
+    def o(precision, scale=1.0, guards=0, band=0.0, batch=0, wait=0):
+        return capi.TraceOptions(precision, rays, scene.jitter_seed, scale, band, 0, wait, 1, guards, batch)
+
+    _, ms64, e64, img64 = run(o(capi.FP64), True, 2)
+    _, _, e64h, img64h = run(o(capi.FP64, 0.5), True, 0)
+    _, ms32, e32, img32 = run(o(capi.FP32), True, 5)
+    print(json.dumps({"variant": "fp64", "ms": ms64}), flush=True)
+    print(json.dumps({"variant": "fp32 (no guards at all)", "ms": ms32,
+                      "vs_fp64": endpoint_error(e32, e64, img32, img64),
+                      "vs_fp64_half": endpoint_error(e32, e64h, img32, img64h)}), flush=True)
+    G = capi
+    variants = [
+        ("all guards, band 0.5, batch 16", dict()),
+        ("all guards, batch 1 (no batching)", dict(batch=1)),
+        ("all guards, batch 32", dict(batch=32)),
+        ("all guards, band 0.7", dict(band=0.7)),
+        ("all guards, band 0.85", dict(band=0.85)),
+        ("motion + psi only", dict(guards=G.GUARD_MOTION | G.GUARD_PSI)),
+        ("motion + horizon + psi", dict(guards=G.GUARD_MOTION | G.GUARD_HORIZON | G.GUARD_PSI)),
+        ("motion + turning points + psi", dict(guards=G.GUARD_MOTION | G.GUARD_RADIAL | G.GUARD_POLAR | G.GUARD_PSI)),
+        ("no motion guard", dict(guards=G.GUARD_ALL & ~G.GUARD_MOTION)),
+    ]
+    for name, kw in variants:
+        s, ms, e, img = run(o(capi.MIXED, **kw), True, 5)
+        print(json.dumps({"variant": name, "ms": ms, "over_fp64": ms64 / ms,
+                          "fp64_steps": s.fp64Steps, "steps": s.steps, "horizon": s.fp64Horizon,
+                          "radial": s.fp64Radial, "polar": s.fp64Polar, "rounds": s.fp64Rounds,
+                          "vs_fp64": endpoint_error(e, e64, img, img64),
+                          "vs_fp64_half": endpoint_error(e, e64h, img, img64h)}), flush=True)
+    lib.artfCudaDestroy(ctx)
 
 
 def profile_case(args):
@@ -206,6 +271,9 @@ def main():
     if args.profile:
         profile_case(args)
         return
+    if args.sweep:
+        sweep(args)
+        return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -230,7 +298,7 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def opts(precision, step_scale=1.0):
-        return capi.TraceOptions(precision, rays, scene.jitter_seed, step_scale, 0.0, 0, 0, 0)
+        return capi.TraceOptions(precision, rays, scene.jitter_seed, step_scale, 0.0, 0, 0, 1)
 
     def timed(precision, steps, warmup):
         o = opts(precision)

@@ -182,7 +182,19 @@ typedef struct ArtfCudaTraceOptions {
     int blockSize;       /* threads a block: 0 picks the tuned value */
     int compactEvery;    /* steps between warp refills: 0 picks the tuned value */
     int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */
+    uint32_t guards;     /* mixed: which FP64 guards run (ARTF_CUDA_GUARD_*); 0 means all */
+    int fp64Batch;       /* mixed: lanes that wait for an FP64 step before a warp runs one; 0 means 16 */
 } ArtfCudaTraceOptions;
+
+/* The mixed trace's FP64 guards. */
+enum {
+    ARTF_CUDA_GUARD_MOTION = 1,   /* constants of motion and the first state from the ray in FP64 */
+    ARTF_CUDA_GUARD_HORIZON = 2,  /* FP64 steps within the band of the outer horizon */
+    ARTF_CUDA_GUARD_RADIAL = 4,   /* the step where du/ds changes sign, in FP64 */
+    ARTF_CUDA_GUARD_POLAR = 8,    /* the step where the axis part of dn/ds changes sign, in FP64 */
+    ARTF_CUDA_GUARD_PSI = 16,     /* compensated summation of psi */
+    ARTF_CUDA_GUARD_ALL = 31
+};
 
 /* Endpoint of each ray (optional output), 32 bytes. */
 typedef struct ArtfCudaRayEnd {
@@ -210,6 +222,8 @@ enum {
 /* What a trace did, counted on the device. */
 typedef struct ArtfCudaTraceStats {
     uint64_t rays, steps, crossings, escapes, fp64Steps;
+    uint64_t fp64Horizon, fp64Radial, fp64Polar; /* mixed: the FP64 steps by their reason */
+    uint64_t fp64Rounds;                         /* mixed: warp rounds of FP64 steps */
     double flops;        /* algorithmic FP32-pipe operations (the counting rule is in lensFlops.h) */
     float ms;            /* device time of the trace kernel(s), CUDA events on the context's stream */
 } ArtfCudaTraceStats;

@@ -23,14 +23,14 @@ def set_inputs(lib, ctx, map_, fluid):
 
 
 def trace(lib, ctx, frame, frame64, precision, jitter=0, seed=0, step_scale=1.0, persistent=0, ends=False,
-          band=0.0):
+          band=0.0, guards=0, batch=0, wait=0):
     """One frame on the device from the context's map and fluid: (H, W, 4) HDR, the ray ends, the stats."""
     torch = _torch()
     w, h = frame.size[0], frame.size[1]
     rays = jitter if jitter else frame.size[2] ** 2
     hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     e = torch.empty((w * h * rays * 32,), dtype=torch.uint8, device="cuda") if ends else None
-    opts = capi.TraceOptions(precision, jitter, seed, step_scale, band, 0, 0, persistent)
+    opts = capi.TraceOptions(precision, jitter, seed, step_scale, band, 0, wait, persistent, guards, batch)
     stats = capi.TraceStats()
     capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64) if frame64 is not None else None, None,
                                      None, C.byref(opts), hdr.data_ptr(), e.data_ptr() if ends else None,
@@ -58,6 +58,21 @@ def trace_rays(lib, ctx, frame, frame64, precision, nx, ny, t, step_scale=1.0, e
     if ends:
         return out, np.frombuffer(e.cpu().numpy().tobytes(), END_DTYPE), stats
     return out, stats
+
+
+def pixel_centres(frame):
+    """The image positions of one ray at each pixel's centre, in the reference's float arithmetic
+    (lens.inc:367-369: the eight-pixel group's base column, then the lane)."""
+    w, h = frame.size[0], frame.size[1]
+    x = np.arange(w, dtype=np.int64)
+    y = np.arange(h, dtype=np.int64)
+    half = np.float32(0.5)
+    nx = (np.float32(x & 7).astype(np.float32) + ((x & ~7).astype(np.float32) + half)) * np.float32(frame.image[1]) \
+        - np.float32(1)
+    ny = np.float32(1) - (y.astype(np.float32) + half) * np.float32(frame.image[2])
+    nx = np.broadcast_to(nx.astype(np.float32)[None, :], (h, w))
+    ny = np.broadcast_to(ny.astype(np.float32)[:, None], (h, w))
+    return np.ascontiguousarray(nx).ravel(), np.ascontiguousarray(ny).ravel()
 
 
 def ring_mask(bits: np.ndarray) -> np.ndarray:

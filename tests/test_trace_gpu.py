@@ -123,6 +123,47 @@ def test_mixed_endpoints_against_fp64(lib, ctx):
     assert 0 < stats.fp64Steps < stats.steps
 
 
+def test_pixel_centres_match_the_reference_positions(lib, ctx, golden):
+    """The exact per-ray entry at the helper's pixel centres reproduces the reference's frame."""
+    meta, arrays = golden
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_101x67")
+    g.set_inputs(lib, ctx, m, fluid)
+    nx, ny = g.pixel_centres(frame)
+    rgb, _ = g.trace_rays(lib, ctx, frame, None, capi.EXACT, nx, ny, 0.0)
+    assert np.array_equal(rgb.reshape(arrays["odd_101x67_hdr"].shape), arrays["odd_101x67_hdr"])
+
+
+def test_mixed_scheduler_matches_per_ray_path(lib, ctx):
+    """The warp-batched scheduler changes when FP64 work runs, never what it computes: the frame equals
+    the per-ray path bit for bit, whatever the batch size."""
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    g.set_inputs(lib, ctx, m, fluid)
+    nx, ny = g.pixel_centres(frame)
+    per_ray, ends_list, s_list = g.trace_rays(lib, ctx, frame, frame64, capi.MIXED, nx, ny, 0.0, ends=True)
+    for batch, wait in ((16, 0), (1, 0), (32, 8)):
+        hdr, ends, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, ends=True, batch=batch, wait=wait)
+        assert np.array_equal(hdr[..., :3].reshape(-1, 3).view(np.uint32), per_ray.view(np.uint32)), batch
+        assert np.array_equal(ends["steps"], ends_list["steps"])
+        assert np.array_equal(ends["fp64Steps"], ends_list["fp64Steps"])
+        assert s.fp64Steps == s_list.fp64Steps and s.steps == s_list.steps
+        assert s.fp64Rounds <= s.fp64Horizon + s.fp64Radial + s.fp64Polar
+
+
+def test_mixed_guards_select_their_fp64_work(lib, ctx):
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    g.set_inputs(lib, ctx, m, fluid)
+    _, s_all = g.trace(lib, ctx, frame, frame64, capi.MIXED)
+    assert s_all.fp64Horizon > 0 and s_all.fp64Radial > 0 and s_all.fp64Polar > 0
+    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, guards=capi.GUARD_MOTION | capi.GUARD_PSI)
+    assert s.fp64Steps == 0 and s.fp64Rounds == 0
+    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, guards=capi.GUARD_HORIZON)
+    assert s.fp64Radial == 0 and s.fp64Polar == 0 and s.fp64Horizon > 0
+    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, guards=capi.GUARD_POLAR | capi.GUARD_MOTION)
+    assert s.fp64Radial == 0 and s.fp64Horizon == 0 and s.fp64Polar > 0
+    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, band=0.9)
+    assert s.fp64Horizon < s_all.fp64Horizon
+
+
 def test_host_path_equals_device_path(lib, ctx):
     import ctypes as C
     scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_101x67")
