@@ -68,7 +68,8 @@ class SynthDesc(C.Structure):
 class TraceOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("jitter", C.c_int), ("seed", C.c_uint32), ("stepScale", C.c_float),
                 ("horizonBand", C.c_float), ("blockSize", C.c_int), ("compactEvery", C.c_int),
-                ("persistent", C.c_int), ("guards", C.c_uint32), ("fp64Batch", C.c_int)]
+                ("persistent", C.c_int), ("guards", C.c_uint32), ("fp64Batch", C.c_int),
+                ("refillBatch", C.c_int)]
 
 
 GUARD_MOTION, GUARD_HORIZON, GUARD_RADIAL, GUARD_POLAR, GUARD_PSI, GUARD_ALL = 1, 2, 4, 8, 16, 31

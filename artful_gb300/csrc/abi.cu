@@ -145,6 +145,10 @@ static int checkFrame(const ArtfCudaHoleFrame* f, const ArtfCudaTraceOptions* o)
     if (o->stepScale < 0.f || o->stepScale > 1.f) return fail(ARTF_CUDA_EINVAL, "stepScale out of [0, 1]");
     if (o->guards > ARTF_CUDA_GUARD_ALL) return fail(ARTF_CUDA_EINVAL, "unknown guard bits %#x", o->guards);
     if (o->fp64Batch < 0 || o->fp64Batch > 32) return fail(ARTF_CUDA_EINVAL, "fp64Batch out of 0..32");
+    if (o->refillBatch < 0 || o->refillBatch > 32) return fail(ARTF_CUDA_EINVAL, "refillBatch out of 0..32");
+    if (o->blockSize != 0 && (o->blockSize < 32 || o->blockSize > 256 || o->blockSize % 32))
+        return fail(ARTF_CUDA_EINVAL, "blockSize %d: 0, or a multiple of 32 up to 256", o->blockSize);
+    if (o->compactEvery < 0 || o->compactEvery > 4096) return fail(ARTF_CUDA_EINVAL, "compactEvery out of range");
     if (o->horizonBand < 0.f || o->horizonBand > 1.f) return fail(ARTF_CUDA_EINVAL, "horizonBand out of [0, 1]");
     return ARTF_CUDA_OK;
 }
@@ -244,6 +248,7 @@ extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, 
     l.persistent = options->persistent;
     l.guards = options->guards;
     l.fp64Batch = options->fp64Batch;
+    l.refillBatch = options->refillBatch;
     return runTrace(ctx, l, options->precision, stats);
 }
 

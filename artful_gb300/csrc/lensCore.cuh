@@ -61,6 +61,50 @@ ARTF_HD int32_t truncI(double x) {
 }
 ARTF_HD int32_t clampI(int32_t i, int32_t lo, int32_t hi) { return i < lo ? lo : i > hi ? hi : i; }
 
+/* Division, reciprocal and square roots.  In float these are the plain operations: the unit's flags
+ * decide their rounding (IEEE in the exact trace).  In double, units that define ARTF_FAST_FP64 take the
+ * hardware's 20-bit estimates (PTX rcp.approx.ftz.f64, rsqrt.approx.f64) and refine them by two
+ * Newton-Raphson iterations, each doubling the correct bits (e = 1 - x y, y += y e for the reciprocal;
+ * e = 1 - x y^2, y += y e / 2 for the inverse square root): within an ulp or two of the IEEE result,
+ * for a fraction of the FP64 instructions of the correctly rounded sequences.  Operands here are
+ * normal and positive where square roots are taken. */
+#if defined(__CUDA_ARCH__) && defined(ARTF_FAST_FP64)
+__device__ __forceinline__ double recipR(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+__device__ __forceinline__ double invSqrtR(double x) {
+    double y;
+    asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x * y, y, 1.0);
+    y = fma(y * .5, e, y);
+    e = fma(-x * y, y, 1.0);
+    return fma(y * .5, e, y);
+}
+__device__ __forceinline__ double divR(double a, double b) { return a * recipR(b); }
+#else
+ARTF_HD double recipR(double x) { return 1.0 / x; }
+ARTF_HD double invSqrtR(double x) { return 1.0 / sqrt(x); }
+ARTF_HD double divR(double a, double b) { return a / b; }
+#endif
+ARTF_HD float recipR(float x) { return 1.f / x; }
+ARTF_HD float invSqrtR(float x) { return 1.f / sqrtf(x); }
+ARTF_HD float divR(float a, float b) { return a / b; }
+/* a / sqrt(x), and sqrt(x) itself */
+ARTF_HD float divSqrtR(float a, float x) { return a / sqrtf(x); }
+#if defined(__CUDA_ARCH__) && defined(ARTF_FAST_FP64)
+__device__ __forceinline__ double divSqrtR(double a, double x) { return a * invSqrtR(x); }
+__device__ __forceinline__ double rootR(double x) { return x * invSqrtR(fmax(x, 1e-300)); }
+#else
+ARTF_HD double divSqrtR(double a, double x) { return a / sqrt(x); }
+ARTF_HD double rootR(double x) { return sqrt(x); }
+#endif
+ARTF_HD float rootR(float x) { return sqrtf(x); }
+
 /* A read of the read-only map or fluid (through the non-coherent path on the GPU). */
 ARTF_HD float fetch(const float* p, int32_t i) {
 #if defined(__CUDA_ARCH__)
@@ -127,30 +171,30 @@ template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R tim
                                             RayState<R>& s) {
     R d[3];
     for (int k = 0; k < 3; ++k) d[k] = f.forward[k] + nx * f.right[k] + ny * f.up[k];
-    const R invLength = R(1) / sqrtR(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const R invLength = invSqrtR(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     for (int k = 0; k < 3; ++k) d[k] = d[k] * invLength;
 
     /* 110-122: light reaching a moving eye from d left, for one at rest, from elsewhere */
     R moved = R(1);
     const R gamma = f.boost[3];
     if (gamma > R(1)) {
-        const R share = gamma / (gamma + R(1));
+        const R share = divR(gamma, gamma + R(1));
         const R cosine = R(0) - (d[0] * f.boost[0] + d[1] * f.boost[1] + d[2] * f.boost[2]);
         const R push = gamma * (R(1) + share * cosine);
-        const R over = R(1) / (gamma * (R(1) + cosine));
+        const R over = recipR(gamma * (R(1) + cosine));
         for (int k = 0; k < 3; ++k) d[k] = (d[k] - f.boost[k] * push) * over;
         moved = over;
     }
 
     const R a = f.a, a2 = a * a, rho = f.place[0], rootDelta = f.place[1], u0 = f.place[2], mu0 = f.place[3];
     const R energy = f.metric[0] - f.metric[1] * d[2];
-    c.invEnergy = R(1) / energy;
+    c.invEnergy = recipR(energy);
     c.xi = R(0) - f.metric[2] * d[2] * c.invEnergy;
     const R xiAxis = f.metric[3] * d[2] * c.invEnergy;
     const R across = rho * d[1] * c.invEnergy;
     const R eta = across * across + mu0 * mu0 * (xiAxis * xiAxis - a2);
     c.big = eta + c.xi * c.xi;
-    c.step = KF(.13089969) * stepScale / sqrtR(maxX(c.big, KF(4.)));
+    c.step = divSqrtR(KF(.13089969) * stepScale, maxX(c.big, KF(4.)));
     c.uA = a2 - c.big;
     const R xiOff = c.xi - a;
     c.uB = KF(3.) * (eta + xiOff * xiOff);
@@ -168,7 +212,7 @@ template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R tim
 
 /* psi' at u (lens.inc:144 DRAG); the denominator is Delta / r^2, kept off zero. */
 template <typename R> ARTF_HD R dragAt(R a, R a2, R xiA, R x) {
-    return (-a) * x * (KF(2.) - xiA * x) / maxX(R(1) - (x + x) + a2 * x * x, KF(1e-3));
+    return divR((-a) * x * (KF(2.) - xiA * x), maxX(R(1) - (x + x) + a2 * x * x, KF(1e-3)));
 }
 
 template <typename R> ARTF_HD R bendAt(const RayConst<R>& c, R x) { return x * (c.uA + x * (c.uB + x * c.uC)); }
@@ -241,7 +285,7 @@ template <typename R> struct Crossing {
 template <typename R> ARTF_HD bool crossingOf(const Frame<R>& f, R rhoScale, const RayConst<R>& c,
                                               const RayState<R>& s, const StepOut<R>& o, Crossing<R>& x) {
     if (!(s.n[2] * o.next.n[2] < R(0))) return false;
-    const R part = s.n[2] / (s.n[2] - o.next.n[2]);
+    const R part = divR(s.n[2], s.n[2] - o.next.n[2]);
     const R hu = part * c.step, hh = hu * hu * KF(.5);
     const R uc = s.u + hu * s.w + hh * o.k1;
     const R rhoCenter = (R(1) - f.inner * uc) * rhoScale;
@@ -263,7 +307,7 @@ template <typename R> ARTF_HD bool crossingOf(const Frame<R>& f, R rhoScale, con
 template <typename R> ARTF_HD R turnsOf(R y, R x) {
     const R ax = absR(x), ay = absR(y);
     const R most = maxX(maxX(ax, ay), KF(1e-20)), least = minX(ax, ay);
-    const R q = least / most, s = q * q;
+    const R q = divR(least, most), s = q * q;
     R r = KF(-.0464964749) * s + KF(.15931422);
     r = r * s - KF(.327622764);
     r = r * s * q + q;
@@ -332,13 +376,13 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
                                               const RayConst<R>& c, const Crossing<R>& x, R& through, R* sum,
                                               R* turnOut) {
     const R turn = turnsOf(x.cy, x.cx) + x.psiC * KF(.15915494);
-    const R rate = ((x.cx * x.vy - x.cy * x.vx) / maxX(x.cx * x.cx + x.cy * x.cy, KF(1e-6)) + x.dragC) * KF(.15915494);
+    const R rate = (divR(x.cx * x.vy - x.cy * x.vx, maxX(x.cx * x.cx + x.cy * x.cy, KF(1e-6))) + x.dragC) * KF(.15915494);
     /* gas seen at a slant is deeper */
-    const R slope = x.wc / x.uc;
+    const R slope = divR(x.wc, x.uc);
     const R speed2 = x.vx * x.vx + x.vy * x.vy + (x.vz * x.vz + slope * slope);
-    const R mu = maxX(absR(x.vz) / sqrtR(speed2), KF(.02));
-    const R slant = f.thickness / R(3) / mu;
-    const R reach = minX(f.discHeight / maxX(absR(x.vz), KF(1e-5)), c.step * KF(1.5));
+    const R mu = maxX(divSqrtR(absR(x.vz), speed2), KF(.02));
+    const R slant = divR(divR(f.thickness, R(3)), mu);
+    const R reach = minX(divR(f.discHeight, maxX(absR(x.vz), KF(1e-5))), c.step * KF(1.5));
     const int32_t mapCount = ARTF_CUDA_MAP_FLOATS, fluidCount = ARTF_CUDA_FLUID_FLOATS;
     const R fluidTime = c.time - f.flow;
 
@@ -375,11 +419,11 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
         const R dusty = rowAt(map, mapCount, ARTF_CUDA_DUST_AT, ARTF_CUDA_DUST_WIDTH, dustRow, turnK - speed0 * c.time);
         const R lit = R(1) - KF(.97) * dusty;
         /* how far from the disc's middle plane, and what the slice stops and gives */
-        const R height = t * (reach / f.discHeight);
+        const R height = t * divR(reach, f.discHeight);
         const R level = maxX(R(1) - x.vz * x.vz * (height * height), R(0));
         density = inside ? density * level : R(0);
         const R depth = slant * density * (R(1) + KF(25.) * dusty);
-        const R alpha = depth / (R(1) + depth);
+        const R alpha = divR(depth, R(1) + depth);
         glow = glow + clear * alpha * (density * lit);
         clear = clear * (R(1) - alpha);
     }
@@ -393,11 +437,11 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
     R light = f.gain * glow * gives;
     if (f.doppler != R(0)) {
         const R safeU = maxX(x.uc, KF(1e-4));
-        const R root = safeU * sqrtR(safeU);
+        const R root = safeU * rootR(safeU);
         const R lift = R(1) + f.a * root;
-        const R spinRate = root / lift;
+        const R spinRate = divR(root, lift);
         const R beneath = maxX(R(1) - KF(3.) * safeU + (KF(2.) * f.a) * root, KF(1e-4));
-        const R shift = sqrtR(beneath) * (c.invEnergy * c.moved) / (lift * (R(1) - spinRate * c.xi));
+        const R shift = divR(rootR(beneath) * (c.invEnergy * c.moved), lift * (R(1) - spinRate * c.xi));
         const R g = R(1) + f.doppler * (shift - R(1));
         const R g2 = g * g;
         light = light * (g2 * g2);
@@ -416,7 +460,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
 
 /* The escape direction in the sky's frame: the last chord's end turned by psi (lens.inc:316-321). */
 template <typename R> ARTF_HD void skyDirection(const R* away, R awayPsi, R* dir) {
-    const R invAway = R(1) / sqrtR(maxX(away[0] * away[0] + away[1] * away[1] + away[2] * away[2], KF(1e-12)));
+    const R invAway = invSqrtR(maxX(away[0] * away[0] + away[1] * away[1] + away[2] * away[2], KF(1e-12)));
     const R psiTurns = awayPsi * KF(.15915494);
     const R sine = sineOf(psiTurns), cosine = sineOf(psiTurns + KF(.25));
     const R x = away[0] * invAway, y = away[1] * invAway, m = away[2] * invAway;

@@ -66,7 +66,7 @@ __device__ __forceinline__ unsigned traceRay(const KernelParams<R>& p, R nx, R n
     rayStart(f, nx, ny, time, p.stepScale, c, s);
     const R a = f.a, a2 = a * a;
     if (a != R(0)) s.drag = dragAt(a, a2, c.xiA, s.u);
-    const R rhoScale = R(1) / (R(1) - f.inner / f.outer);
+    const R rhoScale = recipR(R(1) - divR(f.inner, f.outer));
 
     R raySum[3] = {R(0), R(0), R(0)}, through = R(1);
     unsigned kind = ARTF_CUDA_END_CAP, crossings = 0;
@@ -83,12 +83,12 @@ __device__ __forceinline__ unsigned traceRay(const KernelParams<R>& p, R nx, R n
             const R light = shadeCrossing(f, rhoScale, p.map, p.fluid, c, x, through, raySum, &turn);
             if (light > R(0) && !lit) {
                 lit = true;
-                hitR = R(1) / x.uc;
+                hitR = recipR(x.uc);
                 hitPhi = turn - floorR(turn);
             }
         }
         if (R(0) > o.next.u) {
-            const R part = s.u / (s.u - o.next.u);
+            const R part = divR(s.u, s.u - o.next.u);
             R away[3];
             for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
             const R awayPsi = s.psi + part * (o.next.psi - s.psi);
@@ -143,7 +143,7 @@ template <typename R> __device__ __forceinline__ void tracePixel(const KernelPar
 }
 
 /* One warp per 8 x 4 tile, one thread per pixel. */
-template <typename R> __global__ void __launch_bounds__(128) traceTiles(const KernelParams<R> p) {
+template <typename R> __global__ void __launch_bounds__(256) traceTiles(const KernelParams<R> p) {
     const int lane = threadIdx.x & 31;
     const int tile = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     Tally t;
@@ -155,7 +155,7 @@ template <typename R> __global__ void __launch_bounds__(128) traceTiles(const Ke
 }
 
 /* Persistent: a grid of resident warps that pull tiles from the queue counter until none is left. */
-template <typename R> __global__ void __launch_bounds__(128) traceQueue(const KernelParams<R> p) {
+template <typename R> __global__ void __launch_bounds__(256) traceQueue(const KernelParams<R> p) {
     const int lane = threadIdx.x & 31;
     Tally t;
     for (;;) {
@@ -208,7 +208,7 @@ template <typename R> cudaError_t launchUniform(const TraceLaunch& l, const void
     p.share = l.jitter ? 1.f / (float)l.jitter : l.frame.image[3];
     p.tilesX = ((int)l.frame.size[0] + 7) / 8;
     p.tiles = p.tilesX * (((int)l.frame.size[1] + 3) / 4);
-    const int block = 128;
+    const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
         const RayList list = {l.rayCount, l.rayX, l.rayY, l.rayTime, l.rayRgb};
         traceList<R><<<(l.rayCount + block - 1) / block, block, 0, l.stream>>>(p, list);

@@ -32,6 +32,7 @@ struct TraceLaunch {
     int persistent;
     uint32_t guards;
     int fp64Batch;
+    int refillBatch;
     int smCount;
     cudaStream_t stream;
     /* a list of rays in place of a frame's pixels (rayCount > 0) */

@@ -14,7 +14,8 @@
  *            endpoint's Mino time is formed in FP64 from the step count: neither drifts over 192 steps.
  * The radial and polar sub-steps are independent (u'' depends on u alone, n'' on n alone), so a guard
  * costs FP64 only for the part that needs it.  The disc and sky shading stay in FP32.  Built with the
- * fast FP32 flags; double arithmetic is IEEE throughout.
+ * fast FP32 flags; in double, + - * are IEEE and / and sqrt are refined hardware estimates (within an
+ * ulp or two, lensCore.cuh), as in the plain FP64 trace.
  *
  * Scheduling (traceMixedQueue): the GB300's FP64 pipe is 1/72 of its FP32 pipe, and a warp pays for an
  * FP64 instruction whatever number of its lanes take part.  So FP64 work runs in warp-wide rounds:
@@ -23,6 +24,7 @@
  * without one, or after a bounded wait.  Pixels come from a device queue, a lane at a time, by warp
  * ballot and shuffle.  Every lane computes exactly what the per-ray path (traceRayMixed) computes, in
  * the same order: the schedule changes when, never what. */
+#define ARTF_FAST_FP64 1 /* FP64 division and square roots by refined hardware estimates (lensCore.cuh) */
 #include "lensKernel.cuh"
 
 namespace artf {
@@ -47,6 +49,7 @@ struct MixedParams {
     float uGuard;     /* the horizon band: radial FP64 sub-steps above this u */
     uint32_t guards;  /* ARTF_CUDA_GUARD_* */
     int batch;        /* lanes waiting before a warp runs an FP64 round */
+    int refill;       /* idle lanes before a warp starts new rays (an FP64 set-up each) */
     int maxWait;      /* iterations a lane waits at most */
 };
 
@@ -255,7 +258,7 @@ __device__ __forceinline__ void unitPixel(const MixedParams& p, int u, int& x, i
 }
 
 /* The warp-scheduled trace (see the file's head). */
-__global__ void __launch_bounds__(128) traceMixedQueue(const MixedParams p) {
+__global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -276,7 +279,7 @@ __global__ void __launch_bounds__(128) traceMixedQueue(const MixedParams p) {
         /* (1) refill, batched: the set-up of a ray is FP64 work */
         const unsigned idle = __ballot_sync(full, !live && !exhausted);
         const unsigned liveMask = __ballot_sync(full, live);
-        if (idle && (__popc(idle) >= p.batch || liveMask == 0 || sinceStart >= p.maxWait)) {
+        if (idle && (__popc(idle) >= p.refill || liveMask == 0 || sinceStart >= p.maxWait)) {
             sinceStart = 0;
             const bool needPixel = !live && !exhausted && (unit < 0 || k >= p.rays);
             const unsigned fetch = __ballot_sync(full, needPixel);
@@ -395,11 +398,12 @@ cudaError_t launchMixed(const TraceLaunch& l) {
     p.share = l.jitter ? 1.f / (float)l.jitter : l.frame.image[3];
     p.tilesX = ((int)l.frame.size[0] + 7) / 8;
     p.tiles = p.tilesX * (((int)l.frame.size[1] + 3) / 4);
-    p.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .5f) * l.frame64.spin[1]);
+    p.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * l.frame64.spin[1]);
     p.guards = l.guards ? l.guards : ARTF_CUDA_GUARD_ALL;
-    p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 16;
+    p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 32;
+    p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 16;
     p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
-    const int block = 128;
+    const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
         traceMixedList<<<(l.rayCount + block - 1) / block, block, 0, l.stream>>>(p, l.rayCount, l.rayX, l.rayY,
                                                                                  l.rayTime, l.rayRgb);

@@ -81,8 +81,9 @@ def sweep(args):
         e = np.frombuffer(ends.cpu().numpy().tobytes(), END_DTYPE).copy() if with_ends else None
         return s, (statistics.median(times) if times else s.ms), e, hdr.cpu().numpy().copy()
 
-    def o(precision, scale=1.0, guards=0, band=0.0, batch=0, wait=0):
-        return capi.TraceOptions(precision, rays, scene.jitter_seed, scale, band, 0, wait, 1, guards, batch)
+    def o(precision, scale=1.0, guards=0, band=0.0, batch=0, wait=0, refill=0, block=0):
+        return capi.TraceOptions(precision, rays, scene.jitter_seed, scale, band, block, wait, 1, guards, batch,
+                                 refill)
 
     _, ms64, e64, img64 = run(o(capi.FP64), True, 2)
     _, _, e64h, img64h = run(o(capi.FP64, 0.5), True, 0)
@@ -93,11 +94,18 @@ def sweep(args):
                       "vs_fp64_half": endpoint_error(e32, e64h, img32, img64h)}), flush=True)
     G = capi
     variants = [
-        ("all guards, band 0.5, batch 16", dict()),
-        ("all guards, batch 1 (no batching)", dict(batch=1)),
-        ("all guards, batch 32", dict(batch=32)),
-        ("all guards, band 0.7", dict(band=0.7)),
-        ("all guards, band 0.85", dict(band=0.85)),
+        ("defaults: all guards, band 0.8, batch 32, refill 16, wait 64, block 128", dict()),
+        ("band 0.5", dict(band=0.5)),
+        ("band 0.9", dict(band=0.9)),
+        ("batch 16", dict(batch=16)),
+        ("batch 24", dict(batch=24)),
+        ("refill 8", dict(refill=8)),
+        ("refill 24", dict(refill=24)),
+        ("refill 32", dict(refill=32)),
+        ("wait 16", dict(wait=16)),
+        ("wait 256", dict(wait=256)),
+        ("block 64", dict(block=64)),
+        ("block 256", dict(block=256)),
         ("motion + psi only", dict(guards=G.GUARD_MOTION | G.GUARD_PSI)),
         ("motion + horizon + psi", dict(guards=G.GUARD_MOTION | G.GUARD_HORIZON | G.GUARD_PSI)),
         ("motion + turning points + psi", dict(guards=G.GUARD_MOTION | G.GUARD_RADIAL | G.GUARD_POLAR | G.GUARD_PSI)),

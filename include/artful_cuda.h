@@ -178,12 +178,14 @@ typedef struct ArtfCudaTraceOptions {
     uint32_t seed;       /* of the jitter */
     float stepScale;     /* 1: the reference's step (pi/24 / sqrt(max(K, 4))); 0.5: half steps, with twice
                           * the step cap. 0 means 1 */
-    float horizonBand;   /* mixed: FP64 steps where u > band * (0.995 / r+); 0 means the default (0.5) */
+    float horizonBand;   /* mixed: FP64 radial sub-steps where u > band * (0.995 / r+), i.e. within about
+                          * r+ / band of the hole; 0 means the default 0.8 */
     int blockSize;       /* threads a block: 0 picks the tuned value */
     int compactEvery;    /* steps between warp refills: 0 picks the tuned value */
     int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */
     uint32_t guards;     /* mixed: which FP64 guards run (ARTF_CUDA_GUARD_*); 0 means all */
-    int fp64Batch;       /* mixed: lanes that wait for an FP64 step before a warp runs one; 0 means 16 */
+    int fp64Batch;       /* mixed: lanes that wait for an FP64 sub-step before a warp runs them; 0: 32 */
+    int refillBatch;     /* mixed: idle lanes before a warp starts new rays (FP64 set-ups); 0: 16 */
 } ArtfCudaTraceOptions;
 
 /* The mixed trace's FP64 guards. */

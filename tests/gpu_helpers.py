@@ -23,14 +23,15 @@ def set_inputs(lib, ctx, map_, fluid):
 
 
 def trace(lib, ctx, frame, frame64, precision, jitter=0, seed=0, step_scale=1.0, persistent=0, ends=False,
-          band=0.0, guards=0, batch=0, wait=0):
+          band=0.0, guards=0, batch=0, wait=0, refill=0, block=0):
     """One frame on the device from the context's map and fluid: (H, W, 4) HDR, the ray ends, the stats."""
     torch = _torch()
     w, h = frame.size[0], frame.size[1]
     rays = jitter if jitter else frame.size[2] ** 2
     hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     e = torch.empty((w * h * rays * 32,), dtype=torch.uint8, device="cuda") if ends else None
-    opts = capi.TraceOptions(precision, jitter, seed, step_scale, band, 0, wait, persistent, guards, batch)
+    opts = capi.TraceOptions(precision, jitter, seed, step_scale, band, block, wait, persistent, guards, batch,
+                             refill)
     stats = capi.TraceStats()
     capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64) if frame64 is not None else None, None,
                                      None, C.byref(opts), hdr.data_ptr(), e.data_ptr() if ends else None,
