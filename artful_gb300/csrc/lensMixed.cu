@@ -401,7 +401,7 @@ cudaError_t launchMixed(const TraceLaunch& l) {
     p.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * l.frame64.spin[1]);
     p.guards = l.guards ? l.guards : ARTF_CUDA_GUARD_ALL;
     p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 32;
-    p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 16;
+    p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 32;
     p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {

@@ -185,7 +185,7 @@ typedef struct ArtfCudaTraceOptions {
     int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */
     uint32_t guards;     /* mixed: which FP64 guards run (ARTF_CUDA_GUARD_*); 0 means all */
     int fp64Batch;       /* mixed: lanes that wait for an FP64 sub-step before a warp runs them; 0: 32 */
-    int refillBatch;     /* mixed: idle lanes before a warp starts new rays (FP64 set-ups); 0: 16 */
+    int refillBatch;     /* mixed: idle lanes before a warp starts new rays (FP64 set-ups); 0: 32 */
 } ArtfCudaTraceOptions;
 
 /* The mixed trace's FP64 guards. */

@@ -149,8 +149,6 @@ def test_mixed_scheduler_is_independent_of_batching(lib, ctx):
         assert s.fp64Rounds <= s.fp64Horizon + s.fp64Radial + s.fp64Polar
     nx, ny = g.pixel_centres(frame)
     per_ray, ends_list, s_list = g.trace_rays(lib, ctx, frame, frame64, capi.MIXED, nx, ny, 0.0, ends=True)
-    same = np.all(base[..., :3].reshape(-1, 3) == per_ray, axis=1)
-    assert same.mean() >= 0.99
     lum = base[..., :3].reshape(-1, 3).astype(np.float64).sum(1)
     lum_ray = per_ray.astype(np.float64).sum(1)
     rel = np.abs(lum - lum_ray) / np.maximum(lum_ray, 1e-3)
