@@ -87,6 +87,16 @@ class TraceStats(C.Structure):
                 ("fp64Polar", C.c_uint64), ("fp64Rounds", C.c_uint64), ("flops", C.c_double), ("ms", C.c_float)]
 
 
+class View(C.Structure):
+    _fields_ = [("frame", HoleFrame), ("frame64", HoleFrame64), ("map", C.c_void_p), ("fluid", C.c_void_p),
+                ("hdr", C.c_void_p), ("ends", C.c_void_p)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("blockSize", C.c_int), ("compactEvery", C.c_int), ("fp64Batch", C.c_int), ("refillBatch", C.c_int),
+                ("ms", C.c_float), ("defaultMs", C.c_float), ("trials", C.c_int)]
+
+
 assert C.sizeof(HoleFrame) == 368 and C.sizeof(BlackHoleDesc) == 92 and C.sizeof(Camera) == 44
 assert C.sizeof(RayEnd) == 32
 
@@ -120,6 +130,13 @@ SIGNATURES = {
     "artfCudaHoleTraceRays": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, _vp, C.c_int, C.c_float, C.c_int,
                                         _vp, _vp, _vp, _vp, _vp, P(TraceStats)]),
     "artfCudaProbePeaks": (C.c_int, [_vp, C.c_int, P(C.c_double), P(C.c_double)]),
+    "artfCudaFailAfter": (C.c_int, [_vp, C.c_int]),
+    "artfCudaHoleBatch": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(TraceStats)]),
+    "artfCudaBatchGraphCreate": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(_vp)]),
+    "artfCudaBatchGraphUpdate": (C.c_int, [_vp, P(View), C.c_int]),
+    "artfCudaBatchGraphLaunch": (C.c_int, [_vp, P(TraceStats)]),
+    "artfCudaBatchGraphDestroy": (None, [_vp]),
+    "artfCudaAutotune": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(Tuning)]),
 }
 
 _lib = None

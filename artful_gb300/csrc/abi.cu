@@ -1,8 +1,10 @@
-/* artful_cuda — the C ABI's device side: contexts, uploads and the trace dispatch.  Every entry point
- * checks its arguments and every CUDA call, and reports failure by status, never by abort. */
+/* artful_cuda — the C ABI's device side: contexts, uploads, the trace dispatch, batches of views, their
+ * CUDA graphs and the autotuner.  Every entry point checks its arguments and every CUDA call, and
+ * reports failure by status, never by abort. */
 #include "artful_cuda.h"
 #include "lensFlops.h"
 #include "lensLaunch.h"
+#include "lensMixed.h"
 
 #include <cuda_runtime.h>
 #include <stdarg.h>
@@ -40,6 +42,15 @@ struct ArtfCuda {
     unsigned long long* counters; /* artf::CCount */
     float4* hdr;                  /* the host path's frame buffer */
     size_t hdrPixels;
+    /* the mixed trace's view table: device copy, pinned staging, and when the staging was last read */
+    void* table;
+    void* stage;
+    size_t tableBytes;
+    cudaEvent_t staged;
+    bool stagedPending;
+    ArtfCudaTuning tuned;
+    bool hasTuning;
+    int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
     bool lost;
 };
 
@@ -48,6 +59,24 @@ static int enter(ArtfCuda* ctx) {
     if (!ctx) return fail(ARTF_CUDA_EINVAL, "no context");
     if (ctx->lost) return fail(ARTF_CUDA_ELOST, "the context was lost; destroy it and make another");
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaSetDevice(ctx->device));
+    return ARTF_CUDA_OK;
+}
+
+/* Counts a launch against the injected-fault budget: when it runs out the context is lost, as a device
+ * loss would leave it, without the GPU being touched. */
+static int spendLaunch(ArtfCuda* ctx) {
+    if (ctx->launchesLeft < 0) return ARTF_CUDA_OK;
+    if (ctx->launchesLeft == 0) {
+        ctx->lost = true;
+        return fail(ARTF_CUDA_ELOST, "device loss injected on the host (artfCudaFailAfter)");
+    }
+    --ctx->launchesLeft;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaFailAfter(ArtfCuda* ctx, int launches) {
+    if (!ctx) return fail(ARTF_CUDA_EINVAL, "no context");
+    ctx->launchesLeft = launches < 0 ? -1 : launches;
     return ARTF_CUDA_OK;
 }
 
@@ -67,9 +96,11 @@ extern "C" int artfCudaCreate(int device, ArtfCuda** out) {
     if (!ctx) return fail(ARTF_CUDA_ENOMEM, "host allocation");
     ctx->device = device;
     ctx->smCount = prop.multiProcessorCount;
+    ctx->launchesLeft = -1;
     int status = ARTF_CUDA_OK;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&ctx->start) != cudaSuccess || cudaEventCreate(&ctx->stop) != cudaSuccess)
+        cudaEventCreate(&ctx->start) != cudaSuccess || cudaEventCreate(&ctx->stop) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->staged, cudaEventDisableTiming) != cudaSuccess)
         status = fail(ARTF_CUDA_ELAUNCH, "stream or event creation failed");
     if (!status && (cudaMalloc(&ctx->map, sizeof(float) * ARTF_CUDA_MAP_FLOATS) != cudaSuccess ||
                     cudaMalloc(&ctx->fluid, sizeof(float) * ARTF_CUDA_FLUID_FLOATS) != cudaSuccess ||
@@ -91,8 +122,11 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->fluid);
     cudaFree(ctx->counters);
     cudaFree(ctx->hdr);
+    cudaFree(ctx->table);
+    cudaFreeHost(ctx->stage);
     if (ctx->start) cudaEventDestroy(ctx->start);
     if (ctx->stop) cudaEventDestroy(ctx->stop);
+    if (ctx->staged) cudaEventDestroy(ctx->staged);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     free(ctx);
 }
@@ -133,12 +167,8 @@ static void promoteFrame(const ArtfCudaHoleFrame* f, ArtfCudaHoleFrame64* d) {
         for (int c = 0; c < 4; ++c) dst[i][c] = src[i][c];
 }
 
-static int checkFrame(const ArtfCudaHoleFrame* f, const ArtfCudaTraceOptions* o) {
-    if (!f || !o) return fail(ARTF_CUDA_EINVAL, "frame or options is NULL");
-    if (f->size[0] < 1 || f->size[1] < 1 || f->size[0] > 32768 || f->size[1] > 32768)
-        return fail(ARTF_CUDA_EINVAL, "frame size %u x %u out of range", f->size[0], f->size[1]);
-    if (!o->jitter && (f->size[2] < 1 || f->size[2] > 8))
-        return fail(ARTF_CUDA_EINVAL, "rays a side %u out of 1..8", f->size[2]);
+static int checkOptions(const ArtfCudaTraceOptions* o) {
+    if (!o) return fail(ARTF_CUDA_EINVAL, "options is NULL");
     if (o->jitter < 0 || o->jitter > 256) return fail(ARTF_CUDA_EINVAL, "jitter %d out of 0..256", o->jitter);
     if (o->precision < ARTF_CUDA_EXACT || o->precision > ARTF_CUDA_MIXED)
         return fail(ARTF_CUDA_EINVAL, "unknown precision %d", o->precision);
@@ -153,42 +183,138 @@ static int checkFrame(const ArtfCudaHoleFrame* f, const ArtfCudaTraceOptions* o)
     return ARTF_CUDA_OK;
 }
 
-/* Launches what l describes and, when stats is given, waits and reads the counters and the time. */
-static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCudaTraceStats* stats) {
+static int checkFrame(const ArtfCudaHoleFrame* f, const ArtfCudaTraceOptions* o) {
+    if (!f) return fail(ARTF_CUDA_EINVAL, "frame is NULL");
+    if (int s = checkOptions(o)) return s;
+    if (f->size[0] < 1 || f->size[1] < 1 || f->size[0] > 32768 || f->size[1] > 32768)
+        return fail(ARTF_CUDA_EINVAL, "frame size %u x %u out of range", f->size[0], f->size[1]);
+    if (!o->jitter && (f->size[2] < 1 || f->size[2] > 8))
+        return fail(ARTF_CUDA_EINVAL, "rays a side %u out of 1..8", f->size[2]);
+    return ARTF_CUDA_OK;
+}
+
+/* The launch options of a trace, with the context's tuning where the caller left a value at 0. */
+static artf::TraceLaunch launchOf(const ArtfCuda* ctx, const ArtfCudaTraceOptions* o) {
+    artf::TraceLaunch l;
+    memset(&l, 0, sizeof l);
+    l.jitter = o->jitter;
+    l.seed = o->seed;
+    l.stepScale = o->stepScale > 0.f ? o->stepScale : 1.f;
+    l.horizonBand = o->horizonBand;
+    l.blockSize = o->blockSize;
+    l.compactEvery = o->compactEvery;
+    l.persistent = o->persistent;
+    l.guards = o->guards;
+    l.fp64Batch = o->fp64Batch;
+    l.refillBatch = o->refillBatch;
+    if (ctx->hasTuning && o->precision == ARTF_CUDA_MIXED) {
+        if (!l.blockSize) l.blockSize = ctx->tuned.blockSize;
+        if (!l.compactEvery) l.compactEvery = ctx->tuned.compactEvery;
+        if (!l.fp64Batch) l.fp64Batch = ctx->tuned.fp64Batch;
+        if (!l.refillBatch) l.refillBatch = ctx->tuned.refillBatch;
+    }
     l.counters = ctx->counters;
     l.smCount = ctx->smCount;
     l.stream = ctx->stream;
-    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
-    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-    cudaError_t e = cudaSuccess;
-    switch (precision) {
-    case ARTF_CUDA_EXACT: e = artf::launchExact(l); break;
-    case ARTF_CUDA_FP32: e = artf::launchFast(l); break;
-    case ARTF_CUDA_FP64: e = artf::launchFp64(l); break;
-    default: e = artf::launchMixed(l); break;
-    }
-    if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "trace launch: %s", cudaGetErrorString(e));
-    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
-    if (stats) {
-        unsigned long long c[artf::CCount];
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(c, ctx->counters, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
-        float ms = 0.f;
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventElapsedTime(&ms, ctx->start, ctx->stop));
-        stats->rays = c[artf::CRays];
-        stats->steps = c[artf::CSteps];
-        stats->crossings = c[artf::CCrossings];
-        stats->escapes = c[artf::CEscapes];
-        stats->fp64Steps = precision == ARTF_CUDA_FP64 ? c[artf::CSteps] : c[artf::CFp64Steps];
-        stats->fp64Horizon = c[artf::CFp64Horizon];
-        stats->fp64Radial = c[artf::CFp64Radial];
-        stats->fp64Polar = c[artf::CFp64Polar];
-        stats->fp64Rounds = c[artf::CFp64Rounds];
-        stats->flops = artfFlops(stats->rays, stats->steps, stats->crossings, stats->escapes, l.frame.spin[0] != 0.f,
-                                 l.frame.look[1] != 0.f, l.frame.look[2] > 0.f);
-        stats->ms = ms;
-    }
+    return l;
+}
+
+/* Room for `count` views in the context's table and its staging. */
+static int reserveTable(ArtfCuda* ctx, int count) {
+    const size_t bytes = artf::mixedViewBytes() * (size_t)count;
+    if (bytes <= ctx->tableBytes) return ARTF_CUDA_OK;
+    if (ctx->stagedPending) CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->staged));
+    ctx->stagedPending = false;
+    cudaFree(ctx->table);
+    cudaFreeHost(ctx->stage);
+    ctx->table = ctx->stage = nullptr;
+    ctx->tableBytes = 0;
+    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->table, bytes));
+    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->stage, bytes));
+    ctx->tableBytes = bytes;
     return ARTF_CUDA_OK;
+}
+
+/* Fills the staging table from views; the total queue units in *units. */
+static int fillTable(ArtfCuda* ctx, const artf::TraceLaunch& l, const ArtfCudaView* views, int count,
+                     const ArtfCudaTraceOptions* o, void* stage, int* units) {
+    long long total = 0;
+    for (int i = 0; i < count; ++i) {
+        const ArtfCudaView& v = views[i];
+        if (int s = checkFrame(&v.frame, o)) return s;
+        if (!v.hdr) return fail(ARTF_CUDA_EINVAL, "view %d: hdr is NULL", i);
+        if ((!v.map && !ctx->mapHeld) || (!v.fluid && !ctx->fluidHeld))
+            return fail(ARTF_CUDA_EINVAL, "view %d: no map or fluid, and none set on the context", i);
+        const int n = artf::mixedFillView(l, v.frame, v.frame64, v.map ? v.map : ctx->map, v.fluid ? v.fluid : ctx->fluid,
+                                          (float4*)v.hdr, v.ends, (int)total, (char*)stage + artf::mixedViewBytes() * i);
+        total += n;
+        if (total > 0x7FFFFFFFLL) return fail(ARTF_CUDA_EINVAL, "batch of %lld pixels is too large", total);
+    }
+    *units = (int)total;
+    return ARTF_CUDA_OK;
+}
+
+/* Copies the staged table to the device, after the previous copy has read the staging. */
+static int sendTable(ArtfCuda* ctx, int count) {
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(ctx->table, ctx->stage, artf::mixedViewBytes() * (size_t)count,
+                                               cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->staged, ctx->stream));
+    ctx->stagedPending = true;
+    return ARTF_CUDA_OK;
+}
+
+static int waitStaging(ArtfCuda* ctx) {
+    if (ctx->stagedPending) CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->staged));
+    ctx->stagedPending = false;
+    return ARTF_CUDA_OK;
+}
+
+static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precision, ArtfCudaTraceStats* stats) {
+    unsigned long long c[artf::CCount];
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(c, ctx->counters, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventElapsedTime(&ms, ctx->start, ctx->stop));
+    stats->rays = c[artf::CRays];
+    stats->steps = c[artf::CSteps];
+    stats->crossings = c[artf::CCrossings];
+    stats->escapes = c[artf::CEscapes];
+    stats->fp64Steps = precision == ARTF_CUDA_FP64 ? c[artf::CSteps] : c[artf::CFp64Steps];
+    stats->fp64Horizon = c[artf::CFp64Horizon];
+    stats->fp64Radial = c[artf::CFp64Radial];
+    stats->fp64Polar = c[artf::CFp64Polar];
+    stats->fp64Rounds = c[artf::CFp64Rounds];
+    stats->flops = artfFlops(stats->rays, stats->steps, stats->crossings, stats->escapes, frame.spin[0] != 0.f,
+                             frame.look[1] != 0.f, frame.look[2] > 0.f);
+    stats->ms = ms;
+    return ARTF_CUDA_OK;
+}
+
+/* One frame (or ray list) of any precision: the launch, bracketed by events, and the stats. */
+static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCudaTraceStats* stats) {
+    if (int s = spendLaunch(ctx)) return s;
+    if (precision == ARTF_CUDA_MIXED) {
+        if (int s = reserveTable(ctx, 1)) return s;
+        if (int s = waitStaging(ctx)) return s;
+        const int units = artf::mixedFillView(l, l.frame, l.frame64, l.map, l.fluid, l.hdr, l.ends, 0, ctx->stage);
+        if (int s = sendTable(ctx, 1)) return s;
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units);
+        if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "mixed trace launch: %s", cudaGetErrorString(e));
+    } else {
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+        cudaError_t e = cudaSuccess;
+        switch (precision) {
+        case ARTF_CUDA_EXACT: e = artf::launchExact(l); break;
+        case ARTF_CUDA_FP32: e = artf::launchFast(l); break;
+        default: e = artf::launchFp64(l); break;
+        }
+        if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "trace launch: %s", cudaGetErrorString(e));
+    }
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    return stats ? readStats(ctx, l.frame, precision, stats) : ARTF_CUDA_OK;
 }
 
 extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
@@ -206,15 +332,14 @@ extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* fra
     if (n < 1 || !nx || !ny || !time || !rgb) return fail(ARTF_CUDA_EINVAL, "ray list: n %d or a NULL array", n);
     if (!map && !ctx->mapHeld) return fail(ARTF_CUDA_EINVAL, "no map: pass one or call artfCudaSetMap");
     if (!fluid && !ctx->fluidHeld) return fail(ARTF_CUDA_EINVAL, "no fluid: pass one or call artfCudaSetFluid");
-    artf::TraceLaunch l;
-    memset(&l, 0, sizeof l);
+    artf::TraceLaunch l = launchOf(ctx, &o);
     l.frame = *frame;
     if (frame64) l.frame64 = *frame64;
     else promoteFrame(frame, &l.frame64);
     l.map = map ? map : ctx->map;
     l.fluid = fluid ? fluid : ctx->fluid;
     l.ends = ends;
-    l.stepScale = stepScale > 0.f ? stepScale : 1.f;
+    l.jitter = 0;
     l.rayCount = n;
     l.rayX = nx, l.rayY = ny, l.rayTime = time, l.rayRgb = rgb;
     return runTrace(ctx, l, precision, stats);
@@ -229,8 +354,7 @@ extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, 
     if (!hdr) return fail(ARTF_CUDA_EINVAL, "hdr is NULL");
     if (!map && !ctx->mapHeld) return fail(ARTF_CUDA_EINVAL, "no map: pass one or call artfCudaSetMap");
     if (!fluid && !ctx->fluidHeld) return fail(ARTF_CUDA_EINVAL, "no fluid: pass one or call artfCudaSetFluid");
-    artf::TraceLaunch l;
-    memset(&l, 0, sizeof l);
+    artf::TraceLaunch l = launchOf(ctx, options);
     l.frame = *frame;
     if (frame64) l.frame64 = *frame64;
     else promoteFrame(frame, &l.frame64);
@@ -238,17 +362,6 @@ extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, 
     l.fluid = fluid ? fluid : ctx->fluid;
     l.hdr = (float4*)hdr;
     l.ends = ends;
-    l.counters = ctx->counters;
-    l.jitter = options->jitter;
-    l.seed = options->seed;
-    l.stepScale = options->stepScale > 0.f ? options->stepScale : 1.f;
-    l.horizonBand = options->horizonBand;
-    l.blockSize = options->blockSize;
-    l.compactEvery = options->compactEvery;
-    l.persistent = options->persistent;
-    l.guards = options->guards;
-    l.fp64Batch = options->fp64Batch;
-    l.refillBatch = options->refillBatch;
     return runTrace(ctx, l, options->precision, stats);
 }
 
@@ -275,5 +388,208 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
     CUDA_OR(ARTF_CUDA_ELAUNCH,
             cudaMemcpyAsync(hostHdr, ctx->hdr, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    return ARTF_CUDA_OK;
+}
+
+/* ---- batches ------------------------------------------------------------------------------------- */
+
+static int checkBatch(const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options) {
+    if (!views || count < 1 || count > ARTF_CUDA_MAX_VIEWS)
+        return fail(ARTF_CUDA_EINVAL, "batch of %d views: 1..%d", count, ARTF_CUDA_MAX_VIEWS);
+    if (int s = checkOptions(options)) return s;
+    if (options->precision != ARTF_CUDA_MIXED)
+        return fail(ARTF_CUDA_EINVAL, "batches trace in mixed precision (ARTF_CUDA_MIXED) only");
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int count,
+                                 const ArtfCudaTraceOptions* options, ArtfCudaTraceStats* stats) {
+    int status = enter(ctx);
+    if (status) return status;
+    if ((status = checkBatch(views, count, options))) return status;
+    if ((status = spendLaunch(ctx))) return status;
+    const artf::TraceLaunch l = launchOf(ctx, options);
+    if ((status = reserveTable(ctx, count))) return status;
+    if ((status = waitStaging(ctx))) return status;
+    int units = 0;
+    if ((status = fillTable(ctx, l, views, count, options, ctx->stage, &units))) return status;
+    if ((status = sendTable(ctx, count))) return status;
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units);
+    if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
+}
+
+struct ArtfCudaGraph {
+    ArtfCuda* ctx;
+    int count, units;
+    ArtfCudaTraceOptions options;
+    ArtfCudaHoleFrame first; /* (for the stats' counting rule) */
+    void* table;
+    void* stage;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+extern "C" void artfCudaBatchGraphDestroy(ArtfCudaGraph* g) {
+    if (!g) return;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->table);
+    cudaFreeHost(g->stage);
+    free(g);
+}
+
+extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views, int count,
+                                        const ArtfCudaTraceOptions* options, ArtfCudaGraph** out) {
+    int status = enter(ctx);
+    if (status) return status;
+    if (!out) return fail(ARTF_CUDA_EINVAL, "out is NULL");
+    *out = nullptr;
+    if ((status = checkBatch(views, count, options))) return status;
+    ArtfCudaGraph* g = (ArtfCudaGraph*)calloc(1, sizeof(ArtfCudaGraph));
+    if (!g) return fail(ARTF_CUDA_ENOMEM, "host allocation");
+    g->ctx = ctx;
+    g->count = count;
+    g->options = *options;
+    g->first = views[0].frame;
+    const size_t bytes = artf::mixedViewBytes() * (size_t)count;
+    const artf::TraceLaunch l = launchOf(ctx, options);
+    if (cudaMalloc(&g->table, bytes) != cudaSuccess || cudaMallocHost(&g->stage, bytes) != cudaSuccess) {
+        artfCudaBatchGraphDestroy(g);
+        return fail(ARTF_CUDA_ENOMEM, "graph table allocation");
+    }
+    if ((status = fillTable(ctx, l, views, count, options, g->stage, &g->units))) {
+        artfCudaBatchGraphDestroy(g);
+        return status;
+    }
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaMemcpyAsync(g->table, g->stage, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
+        artf::launchMixedTable(l, g->table, count, g->units);
+        e = cudaStreamEndCapture(ctx->stream, &g->graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        artfCudaBatchGraphDestroy(g);
+        return fail(ARTF_CUDA_ELAUNCH, "graph capture: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaBatchGraphUpdate(ArtfCudaGraph* g, const ArtfCudaView* views, int count) {
+    if (!g) return fail(ARTF_CUDA_EINVAL, "no graph");
+    int status = enter(g->ctx);
+    if (status) return status;
+    if (!views || count != g->count) return fail(ARTF_CUDA_EINVAL, "update needs the graph's %d views", g->count);
+    /* (a launch in flight may still be reading the staging) */
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(g->ctx->stream));
+    const artf::TraceLaunch l = launchOf(g->ctx, &g->options);
+    int units = 0;
+    if ((status = fillTable(g->ctx, l, views, count, &g->options, g->stage, &units))) return status;
+    if (units != g->units) return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
+    g->first = views[0].frame;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* stats) {
+    if (!g) return fail(ARTF_CUDA_EINVAL, "no graph");
+    ArtfCuda* ctx = g->ctx;
+    int status = enter(ctx);
+    if (status) return status;
+    if ((status = spendLaunch(ctx))) return status;
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaGraphLaunch(g->exec, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    return stats ? readStats(ctx, g->first, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
+}
+
+/* ---- the autotuner ------------------------------------------------------------------------------ */
+
+/* Median time of `repeats` launches of the batch already in the context's table. */
+static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int units, int repeats, float* ms) {
+    float times[8];
+    for (int r = -1; r < repeats; ++r) {
+        CUDA_OR(ARTF_CUDA_ELAUNCH,
+                cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units);
+        if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "autotune launch: %s", cudaGetErrorString(e));
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->stop));
+        if (r >= 0) CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventElapsedTime(&times[r], ctx->start, ctx->stop));
+    }
+    for (int i = 1; i < repeats; ++i)
+        for (int j = i; j > 0 && times[j] < times[j - 1]; --j) {
+            const float t = times[j];
+            times[j] = times[j - 1];
+            times[j - 1] = t;
+        }
+    *ms = times[repeats / 2];
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int count,
+                                const ArtfCudaTraceOptions* options, ArtfCudaTuning* result) {
+    int status = enter(ctx);
+    if (status) return status;
+    if (!result) return fail(ARTF_CUDA_EINVAL, "result is NULL");
+    if ((status = checkBatch(views, count, options))) return status;
+    ArtfCudaTraceOptions o = *options;
+    o.blockSize = o.compactEvery = o.fp64Batch = o.refillBatch = 0;
+    ctx->hasTuning = false;
+    artf::TraceLaunch l = launchOf(ctx, &o);
+    if ((status = reserveTable(ctx, count))) return status;
+    if ((status = waitStaging(ctx))) return status;
+    int units = 0;
+    if ((status = fillTable(ctx, l, views, count, &o, ctx->stage, &units))) return status;
+    if ((status = sendTable(ctx, count))) return status;
+
+    /* coordinate descent over the launch shape, from the defaults */
+    static const int blocks[] = {64, 128, 192, 256};
+    static const int waits[] = {16, 32, 64, 128, 256};
+    static const int batches[] = {16, 24, 28, 32};
+    static const int refills[] = {16, 24, 28, 32};
+    int best[4] = {128, 64, 32, 32};
+    const int* values[4] = {blocks, waits, batches, refills};
+    const int counts[4] = {4, 5, 4, 4};
+    const int repeats = 3;
+    float bestMs = 0.f;
+    int trials = 0;
+    l.blockSize = best[0], l.compactEvery = best[1], l.fp64Batch = best[2], l.refillBatch = best[3];
+    if ((status = timeBatch(ctx, l, count, units, repeats, &bestMs))) return status;
+    const float defaultMs = bestMs;
+    ++trials;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int d = 0; d < 4; ++d)
+            for (int c = 0; c < counts[d]; ++c) {
+                int trial[4] = {best[0], best[1], best[2], best[3]};
+                if (values[d][c] == best[d]) continue;
+                trial[d] = values[d][c];
+                l.blockSize = trial[0], l.compactEvery = trial[1], l.fp64Batch = trial[2], l.refillBatch = trial[3];
+                float ms = 0.f;
+                if ((status = timeBatch(ctx, l, count, units, repeats, &ms))) return status;
+                ++trials;
+                if (ms < bestMs * 0.99f) {
+                    bestMs = ms;
+                    memcpy(best, trial, sizeof best);
+                }
+            }
+    ctx->tuned.blockSize = best[0];
+    ctx->tuned.compactEvery = best[1];
+    ctx->tuned.fp64Batch = best[2];
+    ctx->tuned.refillBatch = best[3];
+    ctx->tuned.ms = bestMs;
+    ctx->tuned.defaultMs = defaultMs;
+    ctx->tuned.trials = trials;
+    ctx->hasTuning = true;
+    *result = ctx->tuned;
     return ARTF_CUDA_OK;
 }

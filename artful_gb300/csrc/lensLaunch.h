@@ -46,6 +46,6 @@ struct TraceLaunch {
 cudaError_t launchExact(const TraceLaunch& l);
 cudaError_t launchFast(const TraceLaunch& l);
 cudaError_t launchFp64(const TraceLaunch& l);
-cudaError_t launchMixed(const TraceLaunch& l);
+/* (the mixed trace launches from a view table: lensMixed.h) */
 
 }  // namespace artf

@@ -21,32 +21,41 @@
  * FP64 instruction whatever number of its lanes take part.  So FP64 work runs in warp-wide rounds:
  * lanes that need an FP64 sub-step (or a new ray's FP64 set-up) wait, keeping their FP32 results,
  * while the others keep stepping in FP32; a round runs when `batch` lanes wait, when no lane can move
- * without one, or after a bounded wait.  Pixels come from a device queue, a lane at a time, by warp
- * ballot and shuffle.  Every lane computes exactly what the per-ray path (traceRayMixed) computes, in
- * the same order: the schedule changes when, never what. */
+ * without one, or after a bounded wait.  Pixels of every view of a batch come from one device queue
+ * (work stealing across views of uneven size), a lane at a time, by warp ballot and shuffle.  Every
+ * lane computes exactly what the per-ray path (traceRayMixed) computes, in the same order: the
+ * schedule changes when, never what.  A single frame is a batch of one view. */
 #define ARTF_FAST_FP64 1 /* FP64 division and square roots by refined hardware estimates (lensCore.cuh) */
 #include "lensKernel.cuh"
+#include "lensMixed.h"
+
+#include <string.h>
 
 namespace artf {
-namespace {
 
-struct MixedParams {
+/* A view as the kernel reads it, from the device view table. */
+struct MixedView {
     Frame<float> f;
     Frame<double> d;
-    ArtfCudaHoleFrame h;
+    ArtfCudaHoleFrame h; /* sample positions come from the FP32 frame, as the reference's */
     const float* map;
     const float* fluid;
     float4* hdr;
     ArtfCudaRayEnd* ends;
-    unsigned long long* counters;
-    int jitter;
+    float rhoScale, uGuard, share;
+    int tilesX, units, unitBase, rays, jitter;
     uint32_t seed;
+};
+
+namespace {
+
+struct MixedParams {
+    const MixedView* views;
+    int viewCount;
+    int totalUnits;
+    unsigned long long* counters;
     float stepScale;
     int maxSteps;
-    int rays;
-    float share;
-    int tilesX, tiles;
-    float uGuard;     /* the horizon band: radial FP64 sub-steps above this u */
     uint32_t guards;  /* ARTF_CUDA_GUARD_* */
     int batch;        /* lanes waiting before a warp runs an FP64 round */
     int refill;       /* idle lanes before a warp starts new rays (an FP64 set-up each) */
@@ -72,11 +81,12 @@ __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
 }
 
 /* A ray's start: its constants of motion and first state, in FP64 under the MOTION guard. */
-__device__ __forceinline__ void mixedStart(const MixedParams& p, float nx, float ny, float time, MixedRay& r) {
+__device__ __forceinline__ void mixedStart(const MixedParams& p, const MixedView& v, float nx, float ny, float time,
+                                           MixedRay& r) {
     if (p.guards & ARTF_CUDA_GUARD_MOTION) {
         RayConst<double> cd;
         RayState<double> sd;
-        rayStart(p.d, (double)nx, (double)ny, (double)time, (double)p.stepScale, cd, sd);
+        rayStart(v.d, (double)nx, (double)ny, (double)time, (double)p.stepScale, cd, sd);
         r.c.invEnergy = (float)cd.invEnergy, r.c.xi = (float)cd.xi, r.c.moved = (float)cd.moved;
         r.c.big = (float)cd.big, r.c.step = (float)cd.step, r.c.uA = (float)cd.uA, r.c.uB = (float)cd.uB;
         r.c.uC = (float)cd.uC, r.c.xiA = (float)cd.xiA;
@@ -84,12 +94,12 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, float nx, float
         r.s.u = (float)sd.u, r.s.w = (float)sd.w;
         for (int k = 0; k < 3; ++k) r.s.n[k] = (float)sd.n[k], r.s.v[k] = (float)sd.v[k];
     } else {
-        rayStart(p.f, nx, ny, time, p.stepScale, r.c, r.s);
+        rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
         r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
     }
     r.c.time = time;
     r.s.psi = 0.f;
-    r.s.drag = p.f.a != 0.f ? dragAt(p.f.a, p.f.a * p.f.a, r.c.xiA, r.s.u) : 0.f;
+    r.s.drag = v.f.a != 0.f ? dragAt(v.f.a, v.f.a * v.f.a, r.c.xiA, r.s.u) : 0.f;
     r.psiHi = r.psiLo = 0.f;
     r.through = 1.f;
     r.sum[0] = r.sum[1] = r.sum[2] = 0.f;
@@ -100,59 +110,59 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, float nx, float
 }
 
 /* Which sub-steps of this FP32 step must run again in FP64. */
-__device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedRay& r, const StepOut<float>& o,
-                                           bool& radial, bool& polar, unsigned& reason) {
-    const bool band = (p.guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > p.uGuard;
+__device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedView& v, const MixedRay& r,
+                                           const StepOut<float>& o, bool& radial, bool& polar, unsigned& reason) {
+    const bool band = (p.guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > v.uGuard;
     const bool turnR = (p.guards & ARTF_CUDA_GUARD_RADIAL) && ((r.s.w > 0.f) != (o.next.w > 0.f));
     polar = (p.guards & ARTF_CUDA_GUARD_POLAR) && ((r.s.v[2] > 0.f) != (o.next.v[2] > 0.f));
     radial = band || turnR;
     reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
 }
 
-__device__ __forceinline__ void radialWide(const MixedParams& p, const MixedRay& r, StepOut<float>& o) {
+__device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, StepOut<float>& o) {
     RayState<double> s, next;
     s.u = r.s.u, s.w = r.s.w, s.psi = 0.0, s.drag = r.s.drag;
     double k1;
-    radialStep(p.d.a, wideConst(r), s, next, k1);
+    radialStep(v.d.a, wideConst(r), s, next, k1);
     o.next.u = (float)next.u, o.next.w = (float)next.w, o.next.psi = (float)next.psi, o.next.drag = (float)next.drag;
     o.k1 = (float)k1;
 }
 
-__device__ __forceinline__ void polarWide(const MixedParams& p, const MixedRay& r, StepOut<float>& o) {
+__device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, StepOut<float>& o) {
     RayState<double> s, next;
     for (int k = 0; k < 3; ++k) s.n[k] = r.s.n[k], s.v[k] = r.s.v[k];
     double a1[3];
-    polarStep(p.d.a, wideConst(r), s, next, a1);
+    polarStep(v.d.a, wideConst(r), s, next, a1);
     for (int k = 0; k < 3; ++k) o.next.n[k] = (float)next.n[k], o.next.v[k] = (float)next.v[k], o.a1[k] = (float)a1[k];
 }
 
 /* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
  * (ARTF_CUDA_END_*) + 1, or 0 when the ray goes on. */
-__device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, float rhoScale, MixedRay& r,
+__device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, const MixedView& v, MixedRay& r,
                                                  const StepOut<float>& o) {
-    const Frame<float>& f = p.f;
+    const Frame<float>& f = v.f;
     const bool compensated = p.guards & ARTF_CUDA_GUARD_PSI;
     const float increment = o.next.psi;
     Crossing<float> x;
-    if (crossingOf(f, rhoScale, r.c, r.s, o, x)) {
+    if (crossingOf(f, v.rhoScale, r.c, r.s, o, x)) {
         x.psiC = compensated ? r.psiHi + (r.psiLo + x.part * increment) : r.psiHi + x.part * increment;
         ++r.crossings;
         float turn;
-        const float light = shadeCrossing(f, rhoScale, p.map, p.fluid, r.c, x, r.through, r.sum, &turn);
+        const float light = shadeCrossing(f, v.rhoScale, v.map, v.fluid, r.c, x, r.through, r.sum, &turn);
         if (light > 0.f && !r.lit) {
             r.lit = true;
             r.hitR = 1.f / x.uc;
             r.hitPhi = turn - floorf(turn);
         }
     }
-    const int i = r.i++;
+    ++r.i;
     if (0.f > o.next.u) {
         const float part = r.s.u / (r.s.u - o.next.u);
         float away[3], dir[3];
         for (int k = 0; k < 3; ++k) away[k] = r.s.n[k] + part * (o.next.n[k] - r.s.n[k]);
         const float awayPsi = compensated ? r.psiHi + (r.psiLo + part * increment) : r.psiHi + part * increment;
         skyDirection(away, awayPsi, dir);
-        if (f.stars > 0.f) shadeSky(f, p.map, r.c, dir, r.through, r.sum);
+        if (f.stars > 0.f) shadeSky(f, v.map, r.c, dir, r.through, r.sum);
         /* (the escape's direction and moment travel in the slots the ray no longer needs) */
         r.s.n[0] = dir[0], r.s.n[1] = dir[1], r.s.n[2] = dir[2];
         r.s.w = part;
@@ -169,13 +179,11 @@ __device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, float rho
     }
     r.s = o.next;
     r.s.psi = 0.f;
-    (void)i;
     return r.i >= p.maxSteps ? ARTF_CUDA_END_CAP + 1 : 0u;
 }
 
 /* The end record of a finished ray, and its tallies. */
-__device__ __forceinline__ unsigned mixedFinish(const MixedParams& p, const MixedRay& r, unsigned ended,
-                                                ArtfCudaRayEnd* end, Tally& t) {
+__device__ __forceinline__ unsigned mixedFinish(const MixedRay& r, unsigned ended, ArtfCudaRayEnd* end, Tally& t) {
     unsigned kind = ended - 1;
     if (r.lit) kind |= ARTF_CUDA_END_LIT;
     t.rays += 1;
@@ -211,28 +219,27 @@ __device__ __forceinline__ void countReason(unsigned reason, Reasons& n) {
 }
 
 /* The per-ray path: one ray from start to end, each step's FP64 sub-steps at once. */
-__device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, float nx, float ny, float time, float* sum,
-                                                  ArtfCudaRayEnd* end, Tally& t, Reasons& n) {
+__device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const MixedView& v, float nx, float ny,
+                                                  float time, float* sum, ArtfCudaRayEnd* end, Tally& t, Reasons& n) {
     MixedRay r;
-    mixedStart(p, nx, ny, time, r);
-    const float rhoScale = 1.f / (1.f - p.f.inner / p.f.outer);
+    mixedStart(p, v, nx, ny, time, r);
     unsigned ended = 0;
     while (!ended) {
         StepOut<float> o;
-        nystromStep(p.f.a, r.c, r.s, o);
+        nystromStep(v.f.a, r.c, r.s, o);
         bool radial, polar;
         unsigned reason;
-        mixedNeeds(p, r, o, radial, polar, reason);
-        if (radial) radialWide(p, r, o);
-        if (polar) polarWide(p, r, o);
+        mixedNeeds(p, v, r, o, radial, polar, reason);
+        if (radial) radialWide(v, r, o);
+        if (polar) polarWide(v, r, o);
         if (radial || polar) {
             ++r.wide;
             countReason(reason, n);
         }
-        ended = mixedAdvance(p, rhoScale, r, o);
+        ended = mixedAdvance(p, v, r, o);
     }
     for (int k = 0; k < 3; ++k) sum[k] = sum[k] + r.sum[k];
-    return mixedFinish(p, r, ended, end, t);
+    return mixedFinish(r, ended, end, t);
 }
 
 __device__ __forceinline__ void flushReasons(const Reasons& n, unsigned long long* counters) {
@@ -250,11 +257,15 @@ __device__ __forceinline__ void flushReasons(const Reasons& n, unsigned long lon
     }
 }
 
-/* Pixel unit u (8 x 4 tiles in row-major tile order) to (x, y). */
-__device__ __forceinline__ void unitPixel(const MixedParams& p, int u, int& x, int& y) {
-    const int tile = u >> 5, within = u & 31;
-    x = (tile % p.tilesX) * 8 + (within & 7);
-    y = (tile / p.tilesX) * 4 + (within >> 3);
+/* The view a queue unit belongs to: the last whose first unit is at or below it. */
+__device__ __forceinline__ int viewOf(const MixedParams& p, int unit) {
+    int lo = 0, hi = p.viewCount - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&p.views[mid].unitBase) <= unit) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 /* The warp-scheduled trace (see the file's head). */
@@ -262,11 +273,10 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    const int units = p.tiles * 32;
-    const float rhoScale = 1.f / (1.f - p.f.inner / p.f.outer);
     Tally t;
     Reasons n;
-    int unit = -1, x = 0, y = 0, k = 0;
+    int unit = -1, x = 0, y = 0, k = 0, rays = 1;
+    const MixedView* v = p.views;
     bool exhausted = false, live = false, haveStep = false, waitR = false, waitP = false;
     unsigned reason = 0, bits = 0;
     float pixel[3] = {0.f, 0.f, 0.f};
@@ -281,7 +291,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         const unsigned liveMask = __ballot_sync(full, live);
         if (idle && (__popc(idle) >= p.refill || liveMask == 0 || sinceStart >= p.maxWait)) {
             sinceStart = 0;
-            const bool needPixel = !live && !exhausted && (unit < 0 || k >= p.rays);
+            const bool needPixel = !live && !exhausted && (unit < 0 || k >= rays);
             const unsigned fetch = __ballot_sync(full, needPixel);
             if (fetch) {
                 const int leader = __ffs(fetch) - 1;
@@ -292,19 +302,23 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                     unit = base + __popc(fetch & below);
                     k = 0, bits = 0;
                     pixel[0] = pixel[1] = pixel[2] = 0.f;
-                    if (unit >= units) {
+                    if (unit >= p.totalUnits) {
                         exhausted = true;
                         unit = -1;
                     } else {
-                        unitPixel(p, unit, x, y);
-                        if (x >= p.f.width || y >= p.f.height) k = p.rays; /* (off the image: fetch again) */
+                        v = p.views + viewOf(p, unit);
+                        const int local = unit - v->unitBase, tile = local >> 5, within = local & 31;
+                        x = (tile % v->tilesX) * 8 + (within & 7);
+                        y = (tile / v->tilesX) * 4 + (within >> 3);
+                        rays = v->rays;
+                        if (x >= v->f.width || y >= v->f.height) k = rays; /* (off the image: fetch again) */
                     }
                 }
             }
-            if (!live && unit >= 0 && k < p.rays) {
+            if (!live && unit >= 0 && k < rays) {
                 float nx, ny, moment;
-                samplePosition(p.h, p.jitter, p.seed, x, y, k, &nx, &ny, &moment);
-                mixedStart(p, nx, ny, p.h.disc[2] + p.h.spin[3] * moment, r);
+                samplePosition(v->h, v->jitter, v->seed, x, y, k, &nx, &ny, &moment);
+                mixedStart(p, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
                 live = true;
             }
         } else if (idle) {
@@ -314,8 +328,8 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
 
         /* (2) FP32 steps for the lanes not waiting on FP64 */
         if (live && !haveStep) {
-            nystromStep(p.f.a, r.c, r.s, o);
-            mixedNeeds(p, r, o, waitR, waitP, reason);
+            nystromStep(v->f.a, r.c, r.s, o);
+            mixedNeeds(p, *v, r, o, waitR, waitP, reason);
             haveStep = true;
             if (waitR || waitP) {
                 ++r.wide;
@@ -327,7 +341,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
         if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
             if (waitR) {
-                radialWide(p, r, o);
+                radialWide(*v, r, o);
                 waitR = false;
             }
             sinceRadial = 0;
@@ -337,7 +351,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         }
         if (needP && (__popc(needP) >= p.batch || ready == 0 || sincePolar >= p.maxWait)) {
             if (waitP) {
-                polarWide(p, r, o);
+                polarWide(*v, r, o);
                 waitP = false;
             }
             sincePolar = 0;
@@ -348,15 +362,16 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         /* (4) commit the steps that are complete */
         if (haveStep && !waitR && !waitP) {
             haveStep = false;
-            const unsigned ended = mixedAdvance(p, rhoScale, r, o);
+            const unsigned ended = mixedAdvance(p, *v, r, o);
             if (ended) {
-                const size_t index = (size_t)y * (size_t)p.f.width + (size_t)x;
-                ArtfCudaRayEnd* end = p.ends ? p.ends + index * (size_t)p.rays + (size_t)k : nullptr;
-                bits |= classBits(mixedFinish(p, r, ended, end, t));
+                const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
+                ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)rays + (size_t)k : nullptr;
+                bits |= classBits(mixedFinish(r, ended, end, t));
                 for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
                 live = false;
-                if (++k == p.rays)
-                    p.hdr[index] = make_float4(pixel[0] * p.share, pixel[1] * p.share, pixel[2] * p.share, (float)bits);
+                if (++k == rays)
+                    v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share, pixel[2] * v->share,
+                                                (float)bits);
             }
         }
     }
@@ -364,6 +379,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     flushReasons(n, p.counters);
 }
 
+/* The per-ray entry point: rays at given image positions in the table's first view. */
 __global__ void __launch_bounds__(128) traceMixedList(const MixedParams p, const int count, const float* nx,
                                                       const float* ny, const float* time, float* rgb) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -371,50 +387,75 @@ __global__ void __launch_bounds__(128) traceMixedList(const MixedParams p, const
     Reasons n;
     if (i < count) {
         float sum[3] = {0.f, 0.f, 0.f};
-        traceRayMixed(p, nx[i], ny[i], time[i], sum, p.ends ? p.ends + i : nullptr, t, n);
+        const MixedView& v = p.views[0];
+        traceRayMixed(p, v, nx[i], ny[i], time[i], sum, v.ends ? v.ends + i : nullptr, t, n);
         for (int k = 0; k < 3; ++k) rgb[3 * i + k] = sum[k];
     }
     flushTally(t, p.counters);
     flushReasons(n, p.counters);
 }
 
-}  // namespace
-
-cudaError_t launchMixed(const TraceLaunch& l) {
+MixedParams paramsOf(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits) {
     MixedParams p;
-    p.f.load(l.frame64, l.frame);
-    p.d.load(l.frame64, l.frame);
-    p.h = l.frame;
-    p.map = l.map;
-    p.fluid = l.fluid;
-    p.hdr = l.hdr;
-    p.ends = l.ends;
+    p.views = (const MixedView*)deviceTable;
+    p.viewCount = viewCount;
+    p.totalUnits = totalUnits;
     p.counters = l.counters;
-    p.jitter = l.jitter;
-    p.seed = l.seed;
     p.stepScale = l.stepScale;
     p.maxSteps = l.stepScale < .75f ? 384 : 192;
-    p.rays = l.jitter ? l.jitter : (int)(l.frame.size[2] * l.frame.size[2]);
-    p.share = l.jitter ? 1.f / (float)l.jitter : l.frame.image[3];
-    p.tilesX = ((int)l.frame.size[0] + 7) / 8;
-    p.tiles = p.tilesX * (((int)l.frame.size[1] + 3) / 4);
-    p.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * l.frame64.spin[1]);
     p.guards = l.guards ? l.guards : ARTF_CUDA_GUARD_ALL;
     p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 32;
     p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 32;
     p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
+    return p;
+}
+
+}  // namespace
+
+size_t mixedViewBytes() { return sizeof(MixedView); }
+
+int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
+                  const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, int unitBase, void* slot) {
+    MixedView v;
+    memset(&v, 0, sizeof v);
+    v.f.load(frame64, frame);
+    v.d.load(frame64, frame);
+    v.h = frame;
+    v.map = map;
+    v.fluid = fluid;
+    v.hdr = hdr;
+    v.ends = ends;
+    v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
+    v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * frame64.spin[1]);
+    v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);
+    v.share = l.jitter ? 1.f / (float)l.jitter : frame.image[3];
+    v.jitter = l.jitter;
+    v.seed = l.seed;
+    v.tilesX = ((int)frame.size[0] + 7) / 8;
+    v.units = v.tilesX * (((int)frame.size[1] + 3) / 4) * 32;
+    v.unitBase = unitBase;
+    memcpy(slot, &v, sizeof v);
+    return v.units;
+}
+
+int mixedGrid(const TraceLaunch& l, int totalUnits) {
     const int block = l.blockSize > 0 ? l.blockSize : 128;
-    if (l.rayCount > 0) {
-        traceMixedList<<<(l.rayCount + block - 1) / block, block, 0, l.stream>>>(p, l.rayCount, l.rayX, l.rayY,
-                                                                                 l.rayTime, l.rayRgb);
-        return cudaGetLastError();
-    }
     int perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueue, block, 0);
     int grid = (perSm > 0 ? perSm : 1) * l.smCount;
-    const int needed = (p.tiles * 32 + block - 1) / block;
-    if (grid > needed) grid = needed;
-    traceMixedQueue<<<grid, block, 0, l.stream>>>(p);
+    const int needed = (totalUnits + block - 1) / block;
+    return grid > needed ? needed : (grid < 1 ? 1 : grid);
+}
+
+cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits) {
+    const MixedParams p = paramsOf(l, deviceTable, viewCount, totalUnits);
+    const int block = l.blockSize > 0 ? l.blockSize : 128;
+    if (l.rayCount > 0) {
+        traceMixedList<<<(l.rayCount + 127) / 128, 128, 0, l.stream>>>(p, l.rayCount, l.rayX, l.rayY, l.rayTime,
+                                                                       l.rayRgb);
+        return cudaGetLastError();
+    }
+    traceMixedQueue<<<mixedGrid(l, totalUnits), block, 0, l.stream>>>(p);
     return cudaGetLastError();
 }
 

@@ -390,8 +390,10 @@ def main():
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
 
     cpu = None
+    batch = None
     if rank == 0 and not args.quick:
         cpu = cpu_baseline(scene, frame, map_, fluid, rays)
+        batch = batch_measurement(lib, ctx, args.steps, flush)
 
     lib.artfCudaDestroy(ctx)
     if rank != 0:
@@ -422,7 +424,67 @@ def main():
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if batch:
+        line["batch_64_views"] = batch
     print(json.dumps(line), flush=True)
+
+
+def batch_measurement(lib, ctx, steps, flush):
+    """Configuration 3: 64 views of uneven size, spin, inclination and distance (seed 2), each with its own
+    disc map, traced by one persistent launch captured in a CUDA graph, after the autotuner picked its
+    launch shape; next to the same views as 64 separate launches."""
+    import torch
+    from artful_gb300 import capi, scenes
+    stream = torch.cuda.ExternalStream(lib.artfCudaStream(ctx))
+    views, keep, geodesics = [], [], 0
+    for scene in scenes.config3_views(64, seed=2):
+        frame, frame64, clamped = scenes.frame(scene)
+        m = torch.from_numpy(scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)).cuda()
+        fluid = torch.from_numpy(scenes.unit_fluid()).cuda()
+        hdr = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
+        views.append(capi.View(frame, frame64, m.data_ptr(), fluid.data_ptr(), hdr.data_ptr(), None))
+        keep.append((m, fluid, hdr))
+        geodesics += scene.width * scene.height
+    table = (capi.View * len(views))(*views)
+    opts = capi.TraceOptions(capi.MIXED, 0, 2, 1.0, 0.0, 0, 0, 1)
+    tuning = capi.Tuning()
+    capi.check(lib.artfCudaAutotune(ctx, table, len(views), C.byref(opts), C.byref(tuning)))
+    graph = C.c_void_p()
+    capi.check(lib.artfCudaBatchGraphCreate(ctx, table, len(views), C.byref(opts), C.byref(graph)))
+    stats = capi.TraceStats()
+    capi.check(lib.artfCudaBatchGraphLaunch(graph, C.byref(stats)))
+    times = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.fill_(1)
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            capi.check(lib.artfCudaBatchGraphLaunch(graph, None))
+            stop.record(stream)
+            stop.synchronize()
+            times.append(start.elapsed_time(stop))
+    lib.artfCudaBatchGraphDestroy(graph)
+    ms_batch = statistics.median(times)
+    # the same views one launch each
+    separate = []
+    for _ in range(max(1, steps // 2)):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            for v in views:
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(v.frame), C.byref(v.frame64), v.map, v.fluid,
+                                                 C.byref(opts), v.hdr, None, None))
+            stop.record(stream)
+            stop.synchronize()
+            separate.append(start.elapsed_time(stop))
+    ms_sep = statistics.median(separate)
+    return {"views": len(views), "geodesics": geodesics, "ms_per_batch": ms_batch,
+            "geodesics_per_s": geodesics / (ms_batch * 1e-3), "separate_launches_ms": ms_sep,
+            "batch_over_separate": ms_sep / ms_batch, "fp64_step_share": stats.fp64Steps / max(1, stats.steps),
+            "autotune": {"blockSize": tuning.blockSize, "compactEvery": tuning.compactEvery,
+                         "fp64Batch": tuning.fp64Batch, "refillBatch": tuning.refillBatch,
+                         "tuned_ms": tuning.ms, "default_ms": tuning.defaultMs, "trials": tuning.trials}}
 
 
 def endpoint_error(e, r, img, img_ref):

@@ -155,6 +155,10 @@ void artfCudaDestroy(ArtfCuda* ctx);
  * `version` differs from the one held (0 always copies). */
 int artfCudaSetMap(ArtfCuda* ctx, const float* hostMap, uint64_t version);
 int artfCudaSetFluid(ArtfCuda* ctx, const float* hostFluid, uint64_t version);
+/* Fault injection on the host, for tests of device loss (the reference's artfVulkanSubmitsLeft,
+ * src/render/rendererInternal.h:166-167): after `launches` more launches the context reports
+ * ARTF_CUDA_ELOST, as after a device loss, without the GPU being touched.  -1 turns it off. */
+int artfCudaFailAfter(ArtfCuda* ctx, int launches);
 /* The device copies, for callers that launch on their own buffers. */
 const float* artfCudaDeviceMap(const ArtfCuda* ctx);
 const float* artfCudaDeviceFluid(const ArtfCuda* ctx);
@@ -245,6 +249,50 @@ int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const A
                           const float* map, const float* fluid, int precision, float stepScale, int n, const float* nx,
                           const float* ny, const float* time, float* rgb, ArtfCudaRayEnd* ends,
                           ArtfCudaTraceStats* stats);
+
+/* ---- batches of views (mixed precision) ---------------------------------------------------------- */
+
+/* One view of a batch: its frames, and device pointers to its inputs and outputs. */
+typedef struct ArtfCudaView {
+    ArtfCudaHoleFrame frame;
+    ArtfCudaHoleFrame64 frame64;
+    const float* map;        /* device; NULL: the context's map */
+    const float* fluid;      /* device; NULL: the context's fluid */
+    float* hdr;              /* device: width * height float4 */
+    ArtfCudaRayEnd* ends;    /* device, or NULL */
+} ArtfCudaView;
+
+#define ARTF_CUDA_MAX_VIEWS 4096
+
+/* Traces `count` views of any sizes in one persistent launch (mixed precision): every view's pixels
+ * feed one device work queue that the resident warps steal from, so uneven views balance.  The view
+ * table is copied to the device on the context's stream.  Asynchronous unless stats is given.  No
+ * counterpart in the reference (it draws one view a frame). */
+int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options,
+                      ArtfCudaTraceStats* stats);
+
+/* The same batch captured once in a CUDA graph (table copy, counter reset, launch), then replayed.
+ * Update replaces the views' frames and pointers (same count and sizes) for the next launch.  The graph
+ * owns its device table and pinned staging; the views are copied in at create and update. */
+typedef struct ArtfCudaGraph ArtfCudaGraph;
+int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options,
+                             ArtfCudaGraph** out);
+int artfCudaBatchGraphUpdate(ArtfCudaGraph* graph, const ArtfCudaView* views, int count);
+int artfCudaBatchGraphLaunch(ArtfCudaGraph* graph, ArtfCudaTraceStats* stats);
+void artfCudaBatchGraphDestroy(ArtfCudaGraph* graph);
+
+/* The autotuner: times the batch under candidate launch shapes (threads a block, steps a lane waits at
+ * most before a refill or an FP64 round, the FP64 and refill batch sizes), by coordinate descent from
+ * the defaults, and keeps the fastest in the context: later mixed traces whose options leave these at 0
+ * use it.  Synchronous; a few hundred launches. */
+typedef struct ArtfCudaTuning {
+    int blockSize, compactEvery, fp64Batch, refillBatch;
+    float ms;         /* the best time found */
+    float defaultMs;  /* the defaults' time */
+    int trials;
+} ArtfCudaTuning;
+int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options,
+                     ArtfCudaTuning* result);
 
 /* The same from host memory to host memory: copies the map and fluid (when their versions changed),
  * traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */

@@ -1,0 +1,141 @@
+"""Batches of uneven views in one persistent launch, their CUDA graphs, the autotuner, and device loss
+injected on the host: on a GB300 through the C ABI."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from artful_gb300 import capi, scenes
+from tests import gpu_helpers as g
+
+pytestmark = pytest.mark.gpu
+
+
+def _views(lib, count=6, scale=0.25):
+    """Views of configuration 3 (seed 2), shrunk so the test stays small, each with its own map."""
+    import torch
+    out, keep = [], []
+    for scene in scenes.config3_views(count, seed=2):
+        scene.width = max(8, int(scene.width * scale)) | 1  # (odd widths: ragged tiles)
+        scene.height = max(4, int(scene.height * scale))
+        frame, frame64, clamped = scenes.frame(scene)
+        m = torch.from_numpy(scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)).cuda()
+        fluid = torch.from_numpy(scenes.unit_fluid()).cuda()
+        hdr = torch.zeros((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
+        ends = torch.zeros((scene.width * scene.height * 32,), dtype=torch.uint8, device="cuda")
+        out.append(capi.View(frame, frame64, m.data_ptr(), fluid.data_ptr(), hdr.data_ptr(), ends.data_ptr()))
+        keep.append((scene, m, fluid, hdr, ends))
+    return (capi.View * len(out))(*out), keep
+
+
+def _opts(**kw):
+    o = capi.TraceOptions(capi.MIXED, 0, 0, 1.0, 0.0, 0, 0, 1)
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def test_batch_equals_each_view_alone(lib, ctx):
+    import torch
+    views, keep = _views(lib)
+    stats = capi.TraceStats()
+    capi.check(lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts()), C.byref(stats)))
+    batch = [(hdr.cpu().numpy().copy(), ends.cpu().numpy().copy()) for _, _, _, hdr, ends in keep]
+    assert stats.rays == sum(s.width * s.height for s, *_ in keep)
+    for i, (scene, m, fluid, hdr, ends) in enumerate(keep):
+        hdr.zero_()
+        alone = capi.TraceStats()
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(views[i].frame), C.byref(views[i].frame64), m.data_ptr(),
+                                         fluid.data_ptr(), C.byref(_opts()), hdr.data_ptr(), ends.data_ptr(),
+                                         C.byref(alone)))
+        torch.cuda.synchronize()
+        assert np.array_equal(hdr.cpu().numpy().view(np.uint32), batch[i][0].view(np.uint32)), i
+        assert np.array_equal(ends.cpu().numpy(), batch[i][1]), i
+
+
+def test_graph_replays_and_updates(lib, ctx):
+    import torch
+    views, keep = _views(lib, count=4)
+    graph = C.c_void_p()
+    capi.check(lib.artfCudaBatchGraphCreate(ctx, views, len(views), C.byref(_opts()), C.byref(graph)))
+    try:
+        capi.check(lib.artfCudaBatchGraphLaunch(graph, None))
+        torch.cuda.synchronize()
+        first = [hdr.cpu().numpy().copy() for *_, hdr, _ in keep]
+        for *_, hdr, _ in keep:
+            hdr.zero_()
+        stats = capi.TraceStats()
+        capi.check(lib.artfCudaBatchGraphLaunch(graph, C.byref(stats)))
+        assert all(np.array_equal(a, hdr.cpu().numpy()) for a, (*_, hdr, _) in zip(first, keep))
+        assert stats.rays > 0 and stats.ms > 0
+        # move every eye a little: the replayed graph traces the new frames
+        moved = []
+        for i, (scene, *_) in enumerate(keep):
+            scene.camera = scenes.camera(60.0 + i, 25.0 + i)
+            frame, frame64, _ = scenes.frame(scene)
+            moved.append(capi.View(frame, frame64, views[i].map, views[i].fluid, views[i].hdr, views[i].ends))
+        moved = (capi.View * len(moved))(*moved)
+        capi.check(lib.artfCudaBatchGraphUpdate(graph, moved, len(moved)))
+        capi.check(lib.artfCudaBatchGraphLaunch(graph, None))
+        torch.cuda.synchronize()
+        replayed = [hdr.cpu().numpy().copy() for *_, hdr, _ in keep]
+        capi.check(lib.artfCudaHoleBatch(ctx, moved, len(moved), C.byref(_opts()), None))
+        torch.cuda.synchronize()
+        assert all(np.array_equal(a, hdr.cpu().numpy()) for a, (*_, hdr, _) in zip(replayed, keep))
+        assert not all(np.array_equal(a, b) for a, b in zip(first, replayed))
+        assert lib.artfCudaBatchGraphUpdate(graph, moved, len(moved) - 1) == -1
+    finally:
+        lib.artfCudaBatchGraphDestroy(graph)
+
+
+def test_autotune_picks_a_shape_and_keeps_results(lib, ctx):
+    import torch
+    views, keep = _views(lib, count=5, scale=0.5)
+    capi.check(lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts()), None))
+    torch.cuda.synchronize()
+    before = [hdr.cpu().numpy().copy() for *_, hdr, _ in keep]
+    t = capi.Tuning()
+    capi.check(lib.artfCudaAutotune(ctx, views, len(views), C.byref(_opts()), C.byref(t)))
+    assert t.blockSize in (64, 128, 192, 256) and t.compactEvery >= 16 and 16 <= t.fp64Batch <= 32
+    assert 0 < t.ms <= t.defaultMs * 1.05 and t.trials > 10
+    # the tuned shape changes when the work runs, never the result
+    capi.check(lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts()), None))
+    torch.cuda.synchronize()
+    assert all(np.array_equal(a, hdr.cpu().numpy()) for a, (*_, hdr, _) in zip(before, keep))
+
+
+def test_batch_rejects_bad_requests(lib, ctx):
+    views, keep = _views(lib, count=2)
+    assert lib.artfCudaHoleBatch(ctx, views, 0, C.byref(_opts()), None) == -1
+    assert lib.artfCudaHoleBatch(ctx, views, 2, C.byref(_opts(precision=capi.EXACT)), None) == -1
+    bad = (capi.View * 1)(capi.View(views[0].frame, views[0].frame64, views[0].map, views[0].fluid, None, None))
+    assert lib.artfCudaHoleBatch(ctx, bad, 1, C.byref(_opts()), None) == -1
+    assert b"hdr" in lib.artfCudaLastError()
+
+
+def test_device_loss_injected_on_the_host(lib):
+    """The reference's contract (renderer.h:107-109): after a device loss every call fails and the
+    context must be replaced; a new one works.  The loss is made on the host: no GPU fault."""
+    import torch
+    scene = scenes.golden_scenes()["odd_3x2"]
+    frame, frame64, clamped = scenes.frame(scene)
+    m = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    hdr = torch.empty((2, 3, 4), device="cuda")
+    for attempt in range(2):
+        handle = C.c_void_p()
+        capi.check(lib.artfCudaCreate(0, C.byref(handle)))
+        try:
+            g.set_inputs(lib, handle, m, scenes.unit_fluid())
+            opts = capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 0)
+            if attempt == 0:
+                capi.check(lib.artfCudaFailAfter(handle, 1))
+                assert lib.artfCudaHoleTrace(handle, C.byref(frame), None, None, None, C.byref(opts),
+                                             hdr.data_ptr(), None, None) == 0
+                assert lib.artfCudaHoleTrace(handle, C.byref(frame), None, None, None, C.byref(opts),
+                                             hdr.data_ptr(), None, None) == -6
+                assert lib.artfCudaSetMap(handle, m.ctypes.data, 0) == -6
+            else:
+                assert lib.artfCudaHoleTrace(handle, C.byref(frame), None, None, None, C.byref(opts),
+                                             hdr.data_ptr(), None, None) == 0
+        finally:
+            lib.artfCudaDestroy(handle)
