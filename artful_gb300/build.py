@@ -31,6 +31,7 @@ UNITS = {
     "lensFp64.cu": [],
     "lensMixed.cu": FAST,
     "probe.cu": ["-fmad=true"],
+    "noAlloc.cu": [],
 }
 C_UNITS = ["holeHost.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]

@@ -137,7 +137,10 @@ SIGNATURES = {
     "artfCudaBatchGraphLaunch": (C.c_int, [_vp, P(TraceStats)]),
     "artfCudaBatchGraphDestroy": (None, [_vp]),
     "artfCudaAutotune": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(Tuning)]),
+    "artfCudaHoleBatchNoAlloc": (C.c_int, [P(View), C.c_int, P(TraceOptions), _vp, P(TraceStats)]),
 }
+
+NOALLOC_MAX_VIEWS = 64
 
 _lib = None
 

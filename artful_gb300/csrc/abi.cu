@@ -391,6 +391,14 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
     return ARTF_CUDA_OK;
 }
 
+/* For the other C ABI units (noAlloc.cu): the same error line and argument checks. */
+namespace artf {
+int failWith(int status, const char* message) { return fail(status, "%s", message); }
+int checkTraceFrame(const ArtfCudaHoleFrame* frame, const ArtfCudaTraceOptions* options) {
+    return checkFrame(frame, options);
+}
+}  // namespace artf
+
 /* ---- batches ------------------------------------------------------------------------------------- */
 
 static int checkBatch(const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options) {

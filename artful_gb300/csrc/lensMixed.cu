@@ -46,6 +46,7 @@ struct MixedView {
     int tilesX, units, unitBase, rays, jitter;
     uint32_t seed;
 };
+static_assert(sizeof(MixedView) <= kMixedViewBytesMax, "a view table slot outgrew kMixedViewBytesMax");
 
 namespace {
 

@@ -13,6 +13,9 @@
 
 namespace artf {
 
+/* A table slot never takes more than this (lensMixed.cu checks it at compile time). */
+constexpr size_t kMixedViewBytesMax = 1024;
+
 size_t mixedViewBytes();
 /* Fills one table slot; returns the view's unit count. */
 int mixedFillView(const TraceLaunch& options, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,

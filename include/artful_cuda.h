@@ -281,6 +281,21 @@ int artfCudaBatchGraphUpdate(ArtfCudaGraph* graph, const ArtfCudaView* views, in
 int artfCudaBatchGraphLaunch(ArtfCudaGraph* graph, ArtfCudaTraceStats* stats);
 void artfCudaBatchGraphDestroy(ArtfCudaGraph* graph);
 
+/* A batch trace that allocates nothing, for callers that cannot call cudaMalloc: a host engine or
+ * plug-in framework that owns all device memory through its own allocator, or a render thread that
+ * must not stall on an allocation.  No counterpart in the reference.  It needs no context: it traces on
+ * the current device and on the caller's `stream` (a cudaStream_t, or NULL), and every view's map,
+ * fluid and hdr must be device pointers the caller owns.  Its scratch (the view table and the queue
+ * counters) is one fixed array on each device that loads the library, held until the process exits
+ * (66 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
+ * ARTF_CUDA_EINVAL.  The first call on each device looks up the array's device address there; make it
+ * before any stream capture.  Calls share the array: calls whose work overlaps on the GPU race, so order
+ * them on one stream.  Asynchronous; stats, when given, synchronises the stream and fills the counts
+ * (not ms or flops). */
+#define ARTF_CUDA_NOALLOC_MAX_VIEWS 64
+int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options, void* stream,
+                             ArtfCudaTraceStats* stats);
+
 /* The autotuner: times the batch under candidate launch shapes (threads a block, steps a lane waits at
  * most before a refill or an FP64 round, the FP64 and refill batch sizes), by coordinate descent from
  * the defaults, and keeps the fastest in the context: later mixed traces whose options leave these at 0
