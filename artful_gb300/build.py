@@ -32,8 +32,9 @@ UNITS = {
     "lensMixed.cu": FAST,
     "probe.cu": ["-fmad=true"],
     "noAlloc.cu": [],
+    "post.cu": EXACT,
 }
-C_UNITS = ["holeHost.c"]
+C_UNITS = ["holeHost.c", "renderer.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]
 
 

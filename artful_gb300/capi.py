@@ -138,7 +138,66 @@ SIGNATURES = {
     "artfCudaBatchGraphDestroy": (None, [_vp]),
     "artfCudaAutotune": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(Tuning)]),
     "artfCudaHoleBatchNoAlloc": (C.c_int, [P(View), C.c_int, P(TraceOptions), _vp, P(TraceStats)]),
+    "artfCudaHoleDraw": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, C.c_uint64, _vp, C.c_uint64,
+                                   P(TraceOptions), _vp, _vp, P(TraceStats)]),
+    "artfCudaPostLaunch": (C.c_int, [P(HoleFrame), _vp, P(_vp), _vp, _vp]),
+    # the renderer backend (artful_cuda_renderer.h)
+    "artfCudaNew": (_vp, [_vp]),
+    "artfCudaNewWithReader": (_vp, [_vp, _vp]),
+    "artfCudaRendererReadLight": (C.c_bool, [_vp, _vp]),
+    "artfCudaRendererSetPrecision": (None, [_vp, C.c_int]),
+    "artfCudaRendererContext": (_vp, [_vp]),
+    "artfCudaSceneNew": (_vp, []),
+    "artfCudaSceneFree": (None, [_vp]),
+    "artfCudaSceneSetCamera": (None, [_vp, P(Camera)]),
+    "artfCudaSceneSetBlackHole": (None, [_vp, P(BlackHoleDesc)]),
+    "artfCudaSceneSetHoleMap": (None, [_vp, _vp, _vp, C.c_double]),
+    "artfCudaSceneSetSeed": (None, [_vp, C.c_uint64, C.c_float]),
+    "artfCudaSceneReadHole": (C.c_bool, [_vp, _vp]),
 }
+
+
+class Surface(C.Structure):
+    _fields_ = [("kind", C.c_int), ("a", C.c_void_p), ("b", C.c_void_p)]
+
+
+class RendererOptions(C.Structure):
+    """Layout of Artful's ArtfRendererOptions (include/artful/renderer.h:51-71)."""
+    _fields_ = [("backend", C.c_int), ("surface", Surface), ("width", C.c_int), ("height", C.c_int),
+                ("noVsync", C.c_bool), ("threads", C.c_int), ("simd", C.c_int), ("antialias", C.c_bool),
+                ("hdr", C.c_bool), ("compressTextures", C.c_bool), ("pipelineCache", C.c_char_p)]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("cpuMs", "cullMs", "geometryMs", "rasterMs", "lensMs")] + \
+               [(n, C.c_uint32) for n in ("instancesDrawn", "trianglesBinned", "tilesSkipped", "instancesHidden",
+                                          "traceSamples")] + [("gpuMs", C.c_double), ("shadowMapsDrawn", C.c_uint32)]
+
+
+class Overlay(C.Structure):
+    _fields_ = [("pixels", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("stride", C.c_int),
+                ("partial", C.c_bool), ("damage", C.c_void_p), ("damageCount", C.c_size_t)]
+
+
+class RendererVtbl(C.Structure):
+    """The eight entries of Artful's ArtfRendererVtbl (src/render/rendererInternal.h:146-155)."""
+    _fields_ = [("description", C.CFUNCTYPE(C.c_char_p, C.c_void_p)),
+                ("resize", C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int)),
+                ("setOverlay", C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)),
+                ("draw", C.CFUNCTYPE(C.c_bool, C.c_void_p, C.c_void_p)),
+                ("readPixels", C.CFUNCTYPE(C.c_bool, C.c_void_p, C.c_void_p)),
+                ("pixels", C.CFUNCTYPE(C.c_void_p, C.c_void_p)),
+                ("stats", C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)),
+                ("destroy", C.CFUNCTYPE(None, C.c_void_p))]
+
+
+class RendererHead(C.Structure):
+    """struct ArtfRenderer's head (src/render/rendererInternal.h:157-163)."""
+    _fields_ = [("vt", C.POINTER(RendererVtbl)), ("backend", C.c_int), ("trialFrame", C.c_int),
+                ("trialMs", C.c_double * 2)]
+
+
+assert C.sizeof(RendererOptions) == 64 and C.sizeof(FrameStats) == 80
 
 NOALLOC_MAX_VIEWS = 64
 

@@ -42,6 +42,10 @@ struct ArtfCuda {
     unsigned long long* counters; /* artf::CCount */
     float4* hdr;                  /* the host path's frame buffer */
     size_t hdrPixels;
+    uint32_t* bgra;               /* the draw path's tone-mapped frame */
+    size_t bgraPixels;
+    float* bloom;                 /* three planes of bloomPixels floats */
+    size_t bloomPixels;
     /* the mixed trace's view table: device copy, pinned staging, and when the staging was last read */
     void* table;
     void* stage;
@@ -122,6 +126,8 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->fluid);
     cudaFree(ctx->counters);
     cudaFree(ctx->hdr);
+    cudaFree(ctx->bgra);
+    cudaFree(ctx->bloom);
     cudaFree(ctx->table);
     cudaFreeHost(ctx->stage);
     if (ctx->start) cudaEventDestroy(ctx->start);
@@ -387,6 +393,60 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
         return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH,
             cudaMemcpyAsync(hostHdr, ctx->hdr, sizeof(float4) * pixels, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    return ARTF_CUDA_OK;
+}
+
+/* Grows a device buffer to at least `count` elements of `size` bytes. */
+static int reserve(void** buffer, size_t* held, size_t count, size_t size) {
+    if (count <= *held) return ARTF_CUDA_OK;
+    cudaFree(*buffer);
+    *buffer = nullptr;
+    *held = 0;
+    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(buffer, count * size));
+    *held = count;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
+                                const float* hostMap, uint64_t mapVersion, const float* hostFluid,
+                                uint64_t fluidVersion, const ArtfCudaTraceOptions* options, float* hostHdr,
+                                uint32_t* hostBgra, ArtfCudaTraceStats* stats) {
+    int status = enter(ctx);
+    if (status) return status;
+    if ((status = checkFrame(frame, options))) return status;
+    if ((status = artfCudaSetMap(ctx, hostMap, mapVersion))) return status;
+    if ((status = artfCudaSetFluid(ctx, hostFluid, fluidVersion))) return status;
+    const size_t pixels = (size_t)frame->size[0] * frame->size[1];
+    size_t bloomPixels = 0;
+    for (uint32_t i = 0; i < frame->size[3] && i < ARTF_CUDA_BLOOM_LEVELS; ++i)
+        bloomPixels += (size_t)frame->bloom[i][1] * frame->bloom[i][2];
+    if (frame->size[3] < 1 || bloomPixels == 0) return fail(ARTF_CUDA_EINVAL, "the frame has no bloom levels");
+    if ((status = reserve((void**)&ctx->hdr, &ctx->hdrPixels, pixels, sizeof(float4)))) return status;
+    if ((status = reserve((void**)&ctx->bgra, &ctx->bgraPixels, pixels, sizeof(uint32_t)))) return status;
+    if ((status = reserve((void**)&ctx->bloom, &ctx->bloomPixels, bloomPixels * 3, sizeof(float)))) return status;
+    artf::TraceLaunch l = launchOf(ctx, options);
+    l.frame = *frame;
+    if (frame64) l.frame64 = *frame64;
+    else promoteFrame(frame, &l.frame64);
+    l.map = ctx->map;
+    l.fluid = ctx->fluid;
+    l.hdr = ctx->hdr;
+    /* trace (its own events), then the pyramid and tone map, timed from the trace's start */
+    if ((status = runTrace(ctx, l, options->precision, nullptr))) return status;
+    float* planes[3] = {ctx->bloom, ctx->bloom + bloomPixels, ctx->bloom + 2 * bloomPixels};
+    if ((status = artfCudaPostLaunch(frame, (const float*)ctx->hdr, planes, ctx->bgra, ctx->stream)))
+        return fail(status, "bloom and tone map launch: %s", cudaGetErrorString(cudaGetLastError()));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    if (stats) {
+        if ((status = readStats(ctx, *frame, options->precision, stats))) return status;
+    }
+    if (hostHdr)
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostHdr, ctx->hdr, sizeof(float4) * pixels,
+                                                   cudaMemcpyDeviceToHost, ctx->stream));
+    if (hostBgra)
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostBgra, ctx->bgra, sizeof(uint32_t) * pixels,
+                                                   cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
     return ARTF_CUDA_OK;
 }

@@ -63,7 +63,8 @@ def sweep(args):
     frame, frame64, clamped = scenes.frame(scene)
     map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
     capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
-    capi.check(lib.artfCudaSetFluid(ctx, scenes.unit_fluid().ctypes.data, 1))
+    unit = scenes.unit_fluid()  # (kept alive across the call: the ABI reads it)
+    capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 1))
     w, h, rays = scene.width, scene.height, 4
     hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     ends = torch.empty((w * h * rays * 32,), dtype=torch.uint8, device="cuda")
@@ -133,7 +134,8 @@ def profile_case(args):
     frame, frame64, clamped = scenes.frame(scene)
     map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
     capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
-    capi.check(lib.artfCudaSetFluid(ctx, scenes.unit_fluid().ctypes.data, 1))
+    unit = scenes.unit_fluid()  # (kept alive across the call: the ABI reads it)
+    capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 1))
     hdr = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
     o = capi.TraceOptions(capi.PRECISIONS[args.profile], 4, scene.jitter_seed, 1.0, 0.0, 0, 0, 0)
     for _ in range(2):

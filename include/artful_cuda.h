@@ -250,6 +250,20 @@ int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const A
                           const float* ny, const float* time, float* rgb, ArtfCudaRayEnd* ends,
                           ArtfCudaTraceStats* stats);
 
+/* A whole frame as a renderer backend draws it, from host buffers: the trace, then the bloom pyramid
+ * and the tone map with its dither (src/software/software.c:320-427, src/software/lens.inc:387-440) to
+ * premultiplied BGRA (alpha 255).  Copies back the linear light (width * height float4) to hostHdr and
+ * the BGRA frame (width * height uint32) to hostBgra, each when not NULL.  Synchronous.  stats->ms is
+ * the device time of trace and bloom together (the reference's lensMs). */
+int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
+                     const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
+                     const ArtfCudaTraceOptions* options, float* hostHdr, uint32_t* hostBgra,
+                     ArtfCudaTraceStats* stats);
+/* The bloom and tone map alone, on device buffers: hdr (width * height float4) to bgra, with three bloom
+ * planes of the frame's bloom pixel count (artfCudaHoleFrame's return value), on `stream`. */
+int artfCudaPostLaunch(const ArtfCudaHoleFrame* frame, const float* hdr, float* const bloomPlanes[3], uint32_t* bgra,
+                       void* stream);
+
 /* ---- batches of views (mixed precision) ---------------------------------------------------------- */
 
 /* One view of a batch: its frames, and device pointers to its inputs and outputs. */

@@ -56,6 +56,7 @@ def oracle() -> C.CDLL:
         lib.oracleRender64.argtypes = [vp, vp, vp, vp, C.POINTER(OracleOptions), C.c_int, C.c_uint32, C.c_int,
                                        C.c_int, C.c_int, vp, vp]
         lib.oracleJitter.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.oraclePost.argtypes = [vp, vp, vp]
         lib.oracleThreads.restype = C.c_int
         _oracle = lib
     return _oracle
@@ -98,6 +99,14 @@ def render64(frame, frame64, map_, fluid, jitter=0, seed=0, threads=0, rows=None
     oracle().oracleRender64(C.byref(frame), C.byref(frame64), _ptr(map_), _ptr(fluid),
                             C.byref(OracleOptions(step_scale)), jitter, seed, threads, y0, y1, _ptr(hdr), _ptr(e))
     return (hdr, e) if ends else hdr
+
+
+def post(frame, hdr):
+    """Bloom and tone map of an (H, W, 4) float32 light frame: (H, W) uint32 BGRA."""
+    hdr = np.ascontiguousarray(hdr, np.float32)
+    out = np.zeros(hdr.shape[:2], np.uint32)
+    oracle().oraclePost(C.byref(frame), _ptr(hdr), _ptr(out))
+    return out
 
 
 def jitter_offsets(seed: int, pixel: int, k: int):

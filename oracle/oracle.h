@@ -77,4 +77,7 @@ void oracleRender64(const OracleFrame* h32, const OracleFrame64* h, const float*
  * bits, from a hash of (seed, pixel index, k). */
 void oracleJitter(uint32_t seed, uint32_t pixel, uint32_t k, float* dx, float* dy);
 
+/* The bloom pyramid and tone map of a frame's light (width * height * 4 floats) to BGRA (postOracle.c). */
+void oraclePost(const OracleFrame* h, const float* hdr, uint32_t* bgra);
+
 #endif

@@ -139,6 +139,25 @@ int refPoolThreads(int threads) {
     return n;
 }
 
+/* A whole BGRA frame from the reference's software renderer, through its public API
+ * (artfRendererNew / Draw / ReadPixels, renderer.c:189-254), for a scene holding only this view's hole,
+ * with the given map and fluid field put in place of the scene's own (the same inputs the GPU reads). */
+void refDraw(const RefView* v, const float* map, const float* fluid, int threads, uint32_t* bgra) {
+    ArtfScene* s = artfSceneNew();
+    artfSceneSetCamera(s, &v->camera);
+    artfSceneSetBlackHole(s, &v->desc);
+    memcpy(s->hole.map, map, sizeof(float) * ARTF_HOLE_MAP_FLOATS);
+    memcpy((float*)artfFluidField(s->hole.fluid), fluid, sizeof(float) * ARTF_FLUID_WIDTH * ARTF_FLUID_HEIGHT);
+    ArtfRendererOptions o = artfRendererDefaults(v->width, v->height);
+    o.backend = ARTF_BACKEND_SOFTWARE;
+    o.threads = threads;
+    ArtfRenderer* r = artfRendererNew(&o);
+    artfRendererDraw(r, s);
+    artfRendererReadPixels(r, bgra);
+    artfRendererFree(r);
+    artfSceneFree(s);
+}
+
 /* The reference's ISCO and orbit speed (hole.c:207, hole.c:215). */
 float refIsco(float spin) { return artfHoleIsco(spin); }
 float refOrbitSpeed(float spin, float r) { return artfBlackHoleOrbitSpeed(spin, r); }

@@ -57,6 +57,14 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+def draw_cases():
+    """Views drawn whole through the reference's renderer: (name, scene, bloom, exposure)."""
+    g = scenes.golden_scenes()
+    return [("c1_bloom", g["c1"], 4.5, 1.0), ("c1_dim", g["c1"], 1.0, 0.3),
+            ("moving_2x2_bloom", g["moving_2x2"], 2.0, 1.5), ("odd_101x67_bloom", g["odd_101x67"], 4.5, 1.0),
+            ("odd_3x2", g["odd_3x2"], 4.5, 1.0), ("spinless_3x3_bloom", g["spinless_3x3"], 3.0, 2.0)]
+
+
 def main():
     if not binding.ref_available():
         sys.exit("the reference is not built: make -f oracle/ref.mk")
@@ -137,6 +145,25 @@ def main():
     pix = pix * np.float32(.25)
     arrays["c2_rows"] = pix
     out["c2_rows"] = {"rows": rows, "frame_hex": bytes(frame).hex(), "map_sha256": sha(map_)}
+
+    # whole BGRA frames from the reference's software renderer (artfRendererNew / Draw / ReadPixels),
+    # bloom and tone map included, for a scene holding only the hole, with the synthetic map in place
+    ref.refDraw.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    out["draw"] = {}
+    for name, view, bloom, exposure in draw_cases():
+        d = capi.BlackHoleDesc.from_buffer_copy(view.desc)
+        d.bloom, d.exposure = bloom, exposure
+        view = scenes.Scene(**{**view.__dict__, "desc": d})
+        frame, clamped = ref_frame(ref, view)
+        map_ = scenes.synth_map(lib, clamped, view.seed, view.emissivity)
+        bgra = np.zeros((view.height, view.width), np.uint32)
+        v = RefView(view.camera, d, view.width, view.height)
+        fluid = scenes.unit_fluid()  # (kept alive across the call)
+        ref.refDraw(C.byref(v), map_.ctypes.data, fluid.ctypes.data, 0, bgra.ctypes.data)
+        out["draw"][name] = {"bgra_sha256": sha(bgra), "bloom": bloom, "exposure": exposure, "base": view.name}
+        if bgra.size <= 40000:
+            arrays[f"draw_{name}"] = bgra
+        print("draw", name, sha(bgra)[:16])
 
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:

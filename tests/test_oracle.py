@@ -57,6 +57,32 @@ def test_oracle_jittered_rows_bit_exact(lib, oracle_lib, golden):
         assert np.array_equal(hdr[y, :, :3], arrays["c2_rows"][i])
 
 
+def _draw_case(name):
+    from tests.golden.make_golden import draw_cases
+    for case, view, bloom, exposure in draw_cases():
+        if case == name:
+            d = capi.BlackHoleDesc.from_buffer_copy(view.desc)
+            d.bloom, d.exposure = bloom, exposure
+            return scenes.Scene(**{**view.__dict__, "desc": d})
+    raise KeyError(name)
+
+
+DRAW_CASES = ["c1_bloom", "c1_dim", "moving_2x2_bloom", "odd_101x67_bloom", "odd_3x2", "spinless_3x3_bloom"]
+
+
+@pytest.mark.parametrize("name", DRAW_CASES)
+def test_oracle_bloom_and_tone_map_match_reference_frames(lib, oracle_lib, golden, name):
+    """The whole picture: the oracle's trace, bloom and tone map against the reference renderer's BGRA."""
+    meta, arrays = golden
+    scene = _draw_case(name)
+    frame, _, clamped = scenes.frame(scene)
+    m = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    bgra = binding.post(frame, binding.render32(frame, m, scenes.unit_fluid()))
+    assert hashlib.sha256(bgra.tobytes()).hexdigest() == meta["draw"][name]["bgra_sha256"]
+    if f"draw_{name}" in arrays:
+        assert np.array_equal(bgra, arrays[f"draw_{name}"])
+
+
 def test_oracle_half_step_converges(lib, oracle_lib):
     """The discretisation error of the reference's fixed-step Nystrom: halving the step moves disc hits
     and escape directions far less than a pixel for rays away from the photon ring."""
