@@ -33,6 +33,8 @@ UNITS = {
     "probe.cu": ["-fmad=true"],
     "noAlloc.cu": [],
     "post.cu": EXACT,
+    "lensTangent.cu": [],
+    "lensAdjoint.cu": FAST,
 }
 C_UNITS = ["holeHost.c", "renderer.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]

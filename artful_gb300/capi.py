@@ -97,8 +97,21 @@ class Tuning(C.Structure):
                 ("ms", C.c_float), ("defaultMs", C.c_float), ("trials", C.c_int)]
 
 
+class HoleParams(C.Structure):
+    _fields_ = [(name, C.c_double) for name in ("spin", "inclination", "innerScale", "emissivity", "distance", "fovY",
+                                                "outer", "height", "thickness", "gain", "doppler", "stars", "time")] + \
+               [("seed", C.c_uint64)]
+
+
+class AdjointResult(C.Structure):
+    _fields_ = [("loss", C.c_double), ("grad", C.c_double * 5)]
+
+
+GRAD_FIELDS = 28
+ADJOINT_MIN_CHECKPOINT, ADJOINT_MAX_CHECKPOINT, ADJOINT_MAX_VIEWS = 8, 64, 1024
+
 assert C.sizeof(HoleFrame) == 368 and C.sizeof(BlackHoleDesc) == 92 and C.sizeof(Camera) == 44
-assert C.sizeof(RayEnd) == 32
+assert C.sizeof(RayEnd) == 32 and C.sizeof(HoleParams) == 112 and C.sizeof(AdjointResult) == 48
 
 P = C.POINTER
 _vp = C.c_void_p
@@ -141,6 +154,13 @@ SIGNATURES = {
     "artfCudaHoleDraw": (C.c_int, [_vp, P(HoleFrame), P(HoleFrame64), _vp, C.c_uint64, _vp, C.c_uint64,
                                    P(TraceOptions), _vp, _vp, P(TraceStats)]),
     "artfCudaPostLaunch": (C.c_int, [P(HoleFrame), _vp, P(_vp), _vp, _vp]),
+    # gradients of an image loss in the scene's five parameters
+    "artfCudaHoleParamsScene": (C.c_int, [P(HoleParams), P(Camera), P(BlackHoleDesc)]),
+    "artfCudaHoleParamsFrames": (C.c_int, [P(HoleParams), C.c_int, C.c_int, P(HoleFrame), P(HoleFrame64), _vp]),
+    "artfCudaHoleParamsMap": (C.c_int, [P(HoleParams), _vp]),
+    "artfCudaHoleTangents": (C.c_int, [_vp, P(HoleParams), P(HoleFrame), P(HoleFrame64), _vp, _vp, _vp, _vp]),
+    "artfCudaHoleAdjoint": (C.c_int, [_vp, P(HoleParams), C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp,
+                                      _vp, P(AdjointResult), P(TraceStats)]),
     # the renderer backend (artful_cuda_renderer.h)
     "artfCudaNew": (_vp, [_vp]),
     "artfCudaNewWithReader": (_vp, [_vp, _vp]),

@@ -5,6 +5,7 @@
 #include "lensFlops.h"
 #include "lensLaunch.h"
 #include "lensMixed.h"
+#include "lensTangent.h"
 
 #include <cuda_runtime.h>
 #include <stdarg.h>
@@ -54,6 +55,15 @@ struct ArtfCuda {
     bool stagedPending;
     ArtfCudaTuning tuned;
     bool hasTuning;
+    /* the adjoint's view table (device and pinned staging), block sums and per-view results */
+    void* adjTable;
+    void* adjStage;
+    size_t adjViews;
+    float* adjPartials;
+    size_t adjPartialCount;
+    double* adjResults;
+    double* adjResultsHost;
+    size_t adjResultViews;
     int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
     bool lost;
 };
@@ -130,6 +140,11 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->bloom);
     cudaFree(ctx->table);
     cudaFreeHost(ctx->stage);
+    cudaFree(ctx->adjTable);
+    cudaFreeHost(ctx->adjStage);
+    cudaFree(ctx->adjPartials);
+    cudaFree(ctx->adjResults);
+    cudaFreeHost(ctx->adjResultsHost);
     if (ctx->start) cudaEventDestroy(ctx->start);
     if (ctx->stop) cudaEventDestroy(ctx->stop);
     if (ctx->staged) cudaEventDestroy(ctx->staged);
@@ -448,6 +463,115 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostBgra, ctx->bgra, sizeof(uint32_t) * pixels,
                                                    cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* params, const ArtfCudaHoleFrame* frame,
+                                    const ArtfCudaHoleFrame64* frame64, const double* jacobian, const float* map,
+                                    const float* fluid, double* out) {
+    int status = enter(ctx);
+    if (status) return status;
+    if (!params || !frame || !frame64 || !jacobian || !out) return fail(ARTF_CUDA_EINVAL, "a NULL argument");
+    if (frame->size[0] < 1 || frame->size[1] < 1 || (size_t)frame->size[0] * frame->size[1] > (1u << 24))
+        return fail(ARTF_CUDA_EINVAL, "frame size out of range for the forward-mode reference");
+    if ((!map && !ctx->mapHeld) || (!fluid && !ctx->fluidHeld)) return fail(ARTF_CUDA_EINVAL, "no map or fluid");
+    if ((status = spendLaunch(ctx))) return status;
+    artf::TraceLaunch l;
+    memset(&l, 0, sizeof l);
+    l.frame = *frame;
+    l.frame64 = *frame64;
+    l.map = map ? map : ctx->map;
+    l.fluid = fluid ? fluid : ctx->fluid;
+    l.counters = ctx->counters;
+    l.stream = ctx->stream;
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+    const cudaError_t e = artf::launchTangents(l, jacobian, params->emissivity, out);
+    if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "tangent launch: %s", cudaGetErrorString(e));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    return ARTF_CUDA_OK;
+}
+
+/* Grows the adjoint's table, staging, block sums and results to `count` views of `blocks` blocks. */
+static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks) {
+    if ((size_t)count > ctx->adjViews) {
+        cudaFree(ctx->adjTable);
+        cudaFreeHost(ctx->adjStage);
+        ctx->adjTable = ctx->adjStage = nullptr;
+        ctx->adjViews = 0;
+        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->adjTable, artf::adjointViewBytes() * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->adjStage, artf::adjointViewBytes() * count));
+        ctx->adjViews = (size_t)count;
+    }
+    if ((size_t)count > ctx->adjResultViews) {
+        cudaFree(ctx->adjResults);
+        cudaFreeHost(ctx->adjResultsHost);
+        ctx->adjResults = ctx->adjResultsHost = nullptr;
+        ctx->adjResultViews = 0;
+        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->adjResults, sizeof(double) * 8 * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->adjResultsHost, sizeof(double) * 8 * count));
+        ctx->adjResultViews = (size_t)count;
+    }
+    return reserve((void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float));
+}
+
+extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
+                                   const float* map, const float* fluid, const float* targets, int checkpointEvery,
+                                   float* hdr, float* pixelGrads, ArtfCudaAdjointResult* results,
+                                   ArtfCudaTraceStats* stats) {
+    int status = enter(ctx);
+    if (status) return status;
+    if (!params || !targets || !results) return fail(ARTF_CUDA_EINVAL, "params, targets and results are required");
+    if (count < 1 || count > ARTF_CUDA_ADJOINT_MAX_VIEWS)
+        return fail(ARTF_CUDA_EINVAL, "%d views (1 .. %d)", count, ARTF_CUDA_ADJOINT_MAX_VIEWS);
+    if (width < 1 || height < 1 || width > 16384 || height > 16384 || (size_t)width * height > (1u << 24))
+        return fail(ARTF_CUDA_EINVAL, "size %d x %d out of range", width, height);
+    if (checkpointEvery < ARTF_CUDA_ADJOINT_MIN_CHECKPOINT || checkpointEvery > ARTF_CUDA_ADJOINT_MAX_CHECKPOINT)
+        return fail(ARTF_CUDA_EINVAL, "checkpoint interval %d (%d .. %d)", checkpointEvery,
+                    ARTF_CUDA_ADJOINT_MIN_CHECKPOINT, ARTF_CUDA_ADJOINT_MAX_CHECKPOINT);
+    if ((!map && !ctx->mapHeld) || (!fluid && !ctx->fluidHeld)) return fail(ARTF_CUDA_EINVAL, "no map or fluid");
+    const int pixels = width * height, blocks = artf::adjointBlocks(pixels);
+    if ((status = reserveAdjoint(ctx, count, blocks))) return status;
+    /* (the staging is free: every call ends synchronised) */
+    const size_t slot = artf::adjointViewBytes();
+    for (int v = 0; v < count; ++v) {
+        ArtfCudaHoleFrame frame;
+        double jacobian[ARTF_CUDA_GRAD_FIELDS * 5];
+        if ((status = artfCudaHoleParamsFrames(params + v, width, height, &frame, nullptr, jacobian)))
+            return fail(status, "view %d: parameters out of range", v);
+        if (frame.boost[3] > 1.f) return fail(ARTF_CUDA_EINVAL, "view %d: a moving eye", v);
+        artf::adjointFillView((char*)ctx->adjStage + slot * v, frame, jacobian, params[v].emissivity,
+                              map ? map : ctx->map, fluid ? fluid : ctx->fluid, targets + (size_t)v * pixels * 4,
+                              hdr ? hdr + (size_t)v * pixels * 4 : nullptr,
+                              pixelGrads ? pixelGrads + (size_t)v * pixels * 5 : nullptr);
+    }
+    if ((status = spendLaunch(ctx))) return status;
+    CUDA_OR(ARTF_CUDA_ELAUNCH,
+            cudaMemcpyAsync(ctx->adjTable, ctx->adjStage, slot * count, cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+    const cudaError_t e = artf::launchAdjoint(ctx->adjTable, count, pixels, checkpointEvery, ctx->counters,
+                                              ctx->adjPartials, ctx->adjResults, ctx->stream);
+    if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "adjoint launch: %s", cudaGetErrorString(e));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(ctx->adjResultsHost, ctx->adjResults, sizeof(double) * 8 * count,
+                                               cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long c[artf::CCount];
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(c, ctx->counters, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    for (int v = 0; v < count; ++v) {
+        results[v].loss = ctx->adjResultsHost[v * 8];
+        for (int q = 0; q < 5; ++q) results[v].grad[q] = ctx->adjResultsHost[v * 8 + 1 + q];
+    }
+    if (stats) {
+        float ms = 0.f;
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventElapsedTime(&ms, ctx->start, ctx->stop));
+        memset(stats, 0, sizeof *stats);
+        stats->rays = c[artf::CRays];
+        stats->steps = c[artf::CSteps];
+        stats->crossings = c[artf::CCrossings];
+        stats->escapes = c[artf::CEscapes];
+        stats->ms = ms;
+    }
     return ARTF_CUDA_OK;
 }
 

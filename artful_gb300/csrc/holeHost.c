@@ -231,21 +231,25 @@ static void toLocal64(DVec v, const DVec* basis, DVec er, DVec etheta, DVec ephi
     o[3] = w;
 }
 
-int artfCudaHoleFrame64(const ArtfCudaCamera* c, const ArtfCudaBlackHoleDesc* d, double fluidTime, int width,
-                        int height, ArtfCudaHoleFrame64* out) {
-    if (!c || !d || !out || width < 1 || height < 1) return ARTF_CUDA_EINVAL;
+/* A camera and a hole in double: what the FP64 frame is made from. */
+typedef struct DScene {
+    DVec position, target, up, holePosition, axis, velocity;
+    double fovY, mass, spin, inner, outer, height, shutter, time, thickness, gain, doppler, stars, bloom, exposure;
+    int samples;
+} DScene;
+
+static void frame64Of(const DScene* s, double fluidTime, int width, int height, ArtfCudaHoleFrame64* out) {
     memset(out, 0, sizeof *out);
-    const double a = d->spin, horizon = 1.0 + sqrt(1.0 - a * a);
+    const double a = s->spin, horizon = 1.0 + sqrt(1.0 - a * a);
     DVec basis[3];
     {
-        const DVec axis = dfrom(d->axis);
-        const DVec given = dlength(axis) > 0 ? dnormalize(axis) : dvec(0, 1, 0);
+        const DVec given = dlength(s->axis) > 0 ? dnormalize(s->axis) : dvec(0, 1, 0);
         const DVec other = fabs(given.z) < .9 ? dvec(0, 0, 1) : dvec(1, 0, 0);
         basis[0] = dnormalize(dcross(given, other));
         basis[1] = given;
         basis[2] = dcross(basis[0], basis[1]);
     }
-    DVec eye = dscale(dsub(dfrom(c->position), dfrom(d->position)), 1.0 / d->mass);
+    DVec eye = dscale(dsub(s->position, s->holePosition), 1.0 / s->mass);
     double r = dlength(eye);
     const double least = horizon + .3;
     if (r < least) {
@@ -274,33 +278,45 @@ int artfCudaHoleFrame64(const ArtfCudaCamera* c, const ArtfCudaBlackHoleDesc* d,
     out->place[3] = mu;
     out->spin[0] = a;
     out->spin[1] = .995 / horizon;
-    out->spin[2] = d->discHeight;
-    out->spin[3] = d->shutter;
+    out->spin[2] = s->height;
+    out->spin[3] = s->shutter;
     out->flow[0] = fluidTime;
-    const DVec forward = dnormalize(dsub(dfrom(c->target), dfrom(c->position)));
-    const DVec right = dnormalize(dcross(forward, dfrom(c->up)));
+    const DVec forward = dnormalize(dsub(s->target, s->position));
+    const DVec right = dnormalize(dcross(forward, s->up));
     const DVec up = dcross(right, forward);
-    const double tanY = tan((double)c->fovY * .5), tanX = tanY * (double)width / (double)(height > 1 ? height : 1);
+    const double tanY = tan(s->fovY * .5), tanX = tanY * (double)width / (double)(height > 1 ? height : 1);
     toLocal64(dscale(right, tanX), basis, er, etheta, ephi, 0, out->right);
     toLocal64(dscale(up, tanY), basis, er, etheta, ephi, 0, out->up);
     toLocal64(forward, basis, er, etheta, ephi, 0, out->forward);
-    DVec velocity = dfrom(d->velocity);
+    DVec velocity = s->velocity;
     double speed = dlength(velocity);
     if (speed > .99) velocity = dscale(velocity, .99 / speed);
     if (speed > .99) speed = .99;
     toLocal64(velocity, basis, er, etheta, ephi, 1.0 / sqrt(1.0 - speed * speed), out->boost);
-    out->disc[0] = d->discInner;
-    out->disc[1] = d->discOuter;
-    out->disc[2] = d->time;
-    out->disc[3] = d->discThickness;
-    out->look[0] = d->discGain;
-    out->look[1] = d->doppler;
-    out->look[2] = d->stars;
-    out->look[3] = d->bloom;
-    out->image[0] = d->exposure;
+    out->disc[0] = s->inner;
+    out->disc[1] = s->outer;
+    out->disc[2] = s->time;
+    out->disc[3] = s->thickness;
+    out->look[0] = s->gain;
+    out->look[1] = s->doppler;
+    out->look[2] = s->stars;
+    out->look[3] = s->bloom;
+    out->image[0] = s->exposure;
     out->image[1] = 2.0 / width;
     out->image[2] = 2.0 / height;
-    out->image[3] = 1.0 / ((double)d->samples * d->samples);
+    out->image[3] = 1.0 / ((double)s->samples * s->samples);
+}
+
+int artfCudaHoleFrame64(const ArtfCudaCamera* c, const ArtfCudaBlackHoleDesc* d, double fluidTime, int width,
+                        int height, ArtfCudaHoleFrame64* out) {
+    if (!c || !d || !out || width < 1 || height < 1) return ARTF_CUDA_EINVAL;
+    DScene s;
+    s.position = dfrom(c->position), s.target = dfrom(c->target), s.up = dfrom(c->up), s.fovY = c->fovY;
+    s.holePosition = dfrom(d->position), s.axis = dfrom(d->axis), s.velocity = dfrom(d->velocity);
+    s.mass = d->mass, s.spin = d->spin, s.inner = d->discInner, s.outer = d->discOuter, s.height = d->discHeight;
+    s.shutter = d->shutter, s.time = d->time, s.thickness = d->discThickness, s.gain = d->discGain;
+    s.doppler = d->doppler, s.stars = d->stars, s.bloom = d->bloom, s.exposure = d->exposure, s.samples = d->samples;
+    frame64Of(&s, fluidTime, width, height, out);
     return ARTF_CUDA_OK;
 }
 
@@ -486,4 +502,139 @@ int artfCudaSynthMap(const ArtfCudaSynthDesc* s, float* map) {
     starSky(s->seed, s->stars, map);
     /* dust: none (the memset) */
     return ARTF_CUDA_OK;
+}
+
+/* ---- scenes by their five physical parameters (the adjoint's) ------------------------------------ */
+
+/* The ISCO in double (the same formula as artfCudaIsco, without its rounding to float). */
+static double iscoDouble(double a) {
+    const double a2 = a * a;
+    const double z1 = 1.0 + cubeRootNewton(1.0 - a2) * (cubeRootNewton(1.0 + a) + cubeRootNewton(1.0 - a));
+    const double z2 = sqrt(3.0 * a2 + z1 * z1);
+    const double root = sqrt((3.0 - z1) * (3.0 + z1 + 2.0 * z2));
+    return 3.0 + z2 - (a < 0 ? -root : root);
+}
+
+static DScene paramsScene(const ArtfCudaHoleParams* p, const double* theta) {
+    DScene s;
+    memset(&s, 0, sizeof s);
+    const double a = theta[0], i = theta[1], scale = theta[2], r = theta[4];
+    s.position = dvec(0.0, r * cos(i), r * sin(i));
+    s.target = dvec(0, 0, 0);
+    s.up = dvec(0, 1, 0);
+    s.fovY = p->fovY;
+    s.holePosition = dvec(0, 0, 0);
+    s.axis = dvec(0, 1, 0);
+    s.velocity = dvec(0, 0, 0);
+    s.mass = 1.0, s.spin = a, s.inner = scale * iscoDouble(a), s.outer = p->outer, s.height = p->height;
+    s.shutter = 0.0, s.time = p->time, s.thickness = p->thickness, s.gain = p->gain, s.doppler = p->doppler;
+    s.stars = p->stars, s.bloom = 0.0, s.exposure = 1.0, s.samples = 1;
+    return s;
+}
+
+static void thetaOf(const ArtfCudaHoleParams* p, double* theta) {
+    theta[0] = p->spin, theta[1] = p->inclination, theta[2] = p->innerScale, theta[3] = p->emissivity;
+    theta[4] = p->distance;
+}
+
+/* The scenes the parameters may name: the reference's spin range (|a| <= 0.998), an eye outside the
+ * clamp radius at any inclination, a disc whose inner edge lies inside its outer edge, finite values,
+ * and a margin of the differencing step on every bound. */
+static int paramsValid(const ArtfCudaHoleParams* p) {
+    const double v[] = {p->spin, p->inclination, p->innerScale, p->emissivity, p->distance, p->fovY, p->outer,
+                        p->height, p->thickness, p->gain, p->doppler, p->stars, p->time};
+    for (size_t k = 0; k < sizeof v / sizeof v[0]; ++k)
+        if (!isfinite(v[k])) return 0;
+    if (!(fabs(p->spin) <= .998) || !(p->inclination >= 0.0 && p->inclination <= 3.141592653589793)) return 0;
+    if (!(p->innerScale > 0.0) || !(p->distance >= 4.0) || !(p->fovY > 0.0 && p->fovY < 3.1)) return 0;
+    if (!(p->height > 0.0) || !(p->thickness >= 0.0) || !(p->stars >= 0.0)) return 0;
+    return p->outer > p->innerScale * iscoDouble(p->spin) * 1.001;
+}
+
+int artfCudaHoleParamsScene(const ArtfCudaHoleParams* p, ArtfCudaCamera* camera, ArtfCudaBlackHoleDesc* desc) {
+    if (!p || !camera || !desc || !paramsValid(p)) return ARTF_CUDA_EINVAL;
+    double theta[5];
+    thetaOf(p, theta);
+    const DScene s = paramsScene(p, theta);
+    memset(camera, 0, sizeof *camera);
+    camera->position = vec((float)s.position.x, (float)s.position.y, (float)s.position.z);
+    camera->up = vec(0, 1, 0);
+    camera->fovY = (float)p->fovY;
+    camera->near_ = .1f;
+    *desc = artfCudaBlackHoleDefaults();
+    desc->axis = vec(0, 1, 0);
+    desc->spin = (float)s.spin;
+    desc->discInner = (float)s.inner;
+    desc->discOuter = (float)s.outer;
+    desc->discHeight = (float)s.height;
+    desc->discThickness = (float)s.thickness;
+    desc->discGain = (float)s.gain;
+    desc->doppler = (float)s.doppler;
+    desc->stars = (float)s.stars;
+    desc->bloom = 0.f;
+    desc->exposure = 1.f;
+    desc->time = (float)s.time;
+    desc->samples = 1;
+    return ARTF_CUDA_OK;
+}
+
+/* The frame fields the gradient flows through, in the order of ArtfCudaHoleParams' Jacobian rows. */
+static void gradFields(const ArtfCudaHoleFrame64* f, double* out) {
+    int k = 0;
+    for (int c = 0; c < 3; ++c) out[k++] = f->forward[c];
+    for (int c = 0; c < 3; ++c) out[k++] = f->right[c];
+    for (int c = 0; c < 3; ++c) out[k++] = f->up[c];
+    for (int c = 0; c < 4; ++c) out[k++] = f->metric[c];
+    for (int c = 0; c < 4; ++c) out[k++] = f->place[c];
+    for (int c = 0; c < 3; ++c) out[k++] = f->er[c];
+    for (int c = 0; c < 3; ++c) out[k++] = f->etheta[c];
+    for (int c = 0; c < 3; ++c) out[k++] = f->ephi[c];
+    out[k++] = f->spin[0];
+    out[k++] = f->disc[0];
+}
+
+int artfCudaHoleParamsFrames(const ArtfCudaHoleParams* p, int width, int height, ArtfCudaHoleFrame* f32,
+                             ArtfCudaHoleFrame64* f64, double* jacobian) {
+    if (!p || width < 1 || height < 1 || !paramsValid(p)) return ARTF_CUDA_EINVAL;
+    double theta[5];
+    thetaOf(p, theta);
+    if (f32) {
+        ArtfCudaCamera camera;
+        ArtfCudaBlackHoleDesc desc;
+        artfCudaHoleParamsScene(p, &camera, &desc);
+        if (!artfCudaHoleFrame(&camera, &desc, desc.time, width, height, f32)) return ARTF_CUDA_EINVAL;
+    }
+    if (f64) {
+        const DScene s = paramsScene(p, theta);
+        frame64Of(&s, s.time, width, height, f64);
+    }
+    if (jacobian) {
+        /* central differences of the double frame, step 1e-6 of each parameter's scale */
+        for (int q = 0; q < 5; ++q) {
+            double up[5], down[5];
+            memcpy(up, theta, sizeof up);
+            memcpy(down, theta, sizeof down);
+            const double h = 1e-6 * (fabs(theta[q]) > 1.0 ? fabs(theta[q]) : 1.0);
+            up[q] += h;
+            down[q] -= h;
+            ArtfCudaHoleFrame64 fu, fd;
+            const DScene su = paramsScene(p, up), sd = paramsScene(p, down);
+            frame64Of(&su, su.time, width, height, &fu);
+            frame64Of(&sd, sd.time, width, height, &fd);
+            double gu[ARTF_CUDA_GRAD_FIELDS], gd[ARTF_CUDA_GRAD_FIELDS];
+            gradFields(&fu, gu);
+            gradFields(&fd, gd);
+            for (int k = 0; k < ARTF_CUDA_GRAD_FIELDS; ++k) jacobian[k * 5 + q] = (gu[k] - gd[k]) / (2.0 * h);
+        }
+    }
+    return ARTF_CUDA_OK;
+}
+
+int artfCudaHoleParamsMap(const ArtfCudaHoleParams* p, float* map) {
+    if (!p || !map) return ARTF_CUDA_EINVAL;
+    ArtfCudaCamera camera;
+    ArtfCudaBlackHoleDesc desc;
+    artfCudaHoleParamsScene(p, &camera, &desc);
+    const ArtfCudaSynthDesc synth = {p->seed, desc.discInner, desc.discOuter, desc.spin, (float)p->emissivity, 2000};
+    return artfCudaSynthMap(&synth, map);
 }

@@ -1,0 +1,882 @@
+/* artful_cuda — the adjoint of the trace: the gradient of an image loss with respect to the scene's five
+ * parameters theta = (spin, inclination, inner radius / ISCO, emissivity index q, distance), by
+ * reverse-mode differentiation written out by hand, in FP32.
+ *
+ * Loss of a view: L = sum over pixels and colour channels of (radiance - target)^2 / (3 * pixels), one
+ * ray at each pixel's centre.  Theta reaches the trace through the frame's fields (the eye's basis, the
+ * metric at the eye, the spin, the inner radius: ARTF_CUDA_GRAD_FIELDS of them, whose Jacobian in theta
+ * the host supplies), through the rings' glow (r / inner)^-q and orbit speed, evaluated here from their
+ * formulas, and through the spin in the equations of motion.
+ *
+ * Each thread traces its pixel's ray forward, keeping the ray's state at every step of the current
+ * segment of K steps and a checkpoint at each segment's start; then walks back: the last segment from
+ * what it kept, each earlier one recomputed from its checkpoint.  At each step, in reverse order, it
+ * applies the transposed derivatives of the sky (at the escape), of the disc crossing (its three slices,
+ * the ring's glow and the Doppler shift) and of the Nystrom step's radial and polar parts, accumulating
+ * the adjoints of the constants of motion; at the ray's start it takes them through the set-up to the
+ * frame's fields, and projects those onto theta at once, so a thread carries six sums.  Choices with no
+ * derivative (which texel or star cell, the 0.004 opacity cut-off, the step cap) contribute none: the
+ * pathwise derivative.
+ *
+ * Work layout: a view table in device memory (one entry a view, copied to shared memory by each block),
+ * blocks of 128 threads, grid (blocks a view, views).  Each block writes its six sums; a second kernel
+ * adds them in a fixed order, in double, so the result does not depend on scheduling. */
+#include "lensKernel.cuh"
+#include "lensTangent.h"
+
+#include <string.h>
+
+namespace artf {
+
+struct alignas(16) AdjointView {
+    Frame<float> f;             /* with analyticTables set and the emissivity index */
+    ArtfCudaHoleFrame h;
+    float jacobian[ARTF_CUDA_GRAD_FIELDS][5];
+    const float* map;
+    const float* fluid;
+    const float4* target;
+    float4* hdr;                /* the radiance the forward pass found, or NULL */
+    float* pixelGrads;          /* each pixel's share of the gradient (5 floats a pixel), or NULL */
+    float lossScale;            /* 1 / (3 * pixels) */
+    int pixels;
+};
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxK = ARTF_CUDA_ADJOINT_MAX_CHECKPOINT;
+constexpr int kMaxSteps = 192;
+constexpr int kMaxSegments = kMaxSteps / ARTF_CUDA_ADJOINT_MIN_CHECKPOINT + 1;
+constexpr float kTurn = .15915494f; /* 1 / 2 pi, the reference's constant */
+
+/* Adjoints of what a ray's constants of motion and the frame's scalars feed. */
+struct ConstBar {
+    float step, uA, uB, uC, xiA, big, invEnergy, xi, a, inner, q;
+};
+
+/* ---- the equations' pieces ----------------------------------------------------------------------- */
+
+/* k = x (uA + x (uB + x uC)) taken back. */
+__device__ __forceinline__ void bendBack(const RayConst<float>& c, float x, float kBar, float& xBar, ConstBar& g) {
+    xBar += kBar * (c.uA + x * (2.f * c.uB + 3.f * c.uC * x));
+    g.uA += kBar * x;
+    g.uB += kBar * x * x;
+    g.uC += kBar * x * x * x;
+}
+
+/* psi' = -a x (2 - xiA x) / max(1 - 2x + a^2 x^2, 1e-3) taken back. */
+__device__ __forceinline__ void dragBack(float a, float xiA, float x, float dBar, float& xBar, ConstBar& g) {
+    const float num = -a * x * (2.f - xiA * x);
+    const float raw = 1.f - (x + x) + a * a * x * x;
+    const bool held = !(raw > 1e-3f);
+    const float den = held ? 1e-3f : raw;
+    const float numBar = dBar / den, denBar = held ? 0.f : -numBar * num / den;
+    xBar += numBar * (-a * (2.f - 2.f * xiA * x)) + denBar * (2.f * a * a * x - 2.f);
+    g.a += numBar * (-x * (2.f - xiA * x)) + denBar * 2.f * a * x * x;
+    g.xiA += numBar * a * x * x;
+}
+
+/* n'' = A(n) = (-c nx, -c ny, a^2 nz - c nz), c = K + 2 a^2 nz^2. */
+__device__ __forceinline__ void accelOf(float a, float big, const float* n, float* out) {
+    const float c = big + 2.f * a * a * (n[2] * n[2]);
+    out[0] = -c * n[0], out[1] = -c * n[1], out[2] = a * a * n[2] - c * n[2];
+}
+
+/* A(n) taken back from its adjoint. */
+__device__ __forceinline__ void accelBack(float a, float big, const float* n, const float* outBar, float* nBar,
+                                          ConstBar& g) {
+    const float a2 = a * a, c = big + 2.f * a2 * (n[2] * n[2]);
+    const float cBar = -(n[0] * outBar[0] + n[1] * outBar[1] + n[2] * outBar[2]);
+    nBar[0] += -c * outBar[0];
+    nBar[1] += -c * outBar[1];
+    nBar[2] += (a2 - c) * outBar[2] + cBar * 4.f * a2 * n[2];
+    g.a += 2.f * a * n[2] * outBar[2] + cBar * 4.f * a * n[2] * n[2];
+    g.big += cBar;
+}
+
+/* lens.inc:30-41's polynomial arctangent (in turns): its slopes in y and x. */
+__device__ __forceinline__ void turnsSlope(float y, float x, float& dy, float& dx) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const bool steep = ay > ax;
+    const float most = fmaxf(steep ? ay : ax, 1e-20f), least = steep ? ax : ay;
+    const float q = least / most, s = q * q;
+    const float slope = 1.f + s * (-3.f * .327622764f + s * (5.f * .15931422f + s * (7.f * -.0464964749f)));
+    float sign = steep ? -1.f : 1.f;
+    if (x < 0.f) sign = -sign;
+    if (y < 0.f) sign = -sign;
+    const float k = kTurn * sign * slope;
+    const float dqLeast = 1.f / most, dqMost = -q / most;
+    dx = k * (steep ? dqLeast : dqMost) * (x < 0.f ? -1.f : 1.f);
+    dy = k * (steep ? dqMost : dqLeast) * (y < 0.f ? -1.f : 1.f);
+}
+
+/* lens.inc:44-54's polynomial sine of an angle in turns: its slope. */
+__device__ __forceinline__ float sineSlope(float turns) {
+    float t = turns - floorf(turns + .5f), sign = 1.f;
+    if (t > .25f) t = .5f - t, sign = -sign;
+    if (t < -.25f) t = -.5f - t, sign = -sign;
+    const float x = t * 6.2831853f, x2 = x * x;
+    const float d = 1.f + x2 * (3.f * -.16666667f +
+                                x2 * (5.f * 8.3333333e-3f + x2 * (7.f * -1.9841270e-4f + x2 * (9.f * 2.7557319e-6f))));
+    return sign * 6.2831853f * d;
+}
+
+/* A map row read at a turn (rowAt): its slope in the turn. */
+__device__ __forceinline__ float rowSlope(const float* buffer, int32_t count, int32_t at, int32_t width, int32_t row,
+                                          float turn) {
+    const float pos = (turn - floorf(turn)) * (float)width;
+    const int32_t c0 = truncI(floorf(pos)) & (width - 1), c1 = (c0 + 1) & (width - 1);
+    const int32_t base = at + row * width;
+    const float lo = fetch(buffer, clampI(base + c0, 0, count - 1)), hi = fetch(buffer, clampI(base + c1, 0, count - 1));
+    return (hi - lo) * (float)width;
+}
+
+/* The rings' orbit speed 1 / (2 pi (r^1.5 + a)) at a row, r = inner / span: its slopes in a and inner. */
+__device__ __forceinline__ void speedSlopes(const Frame<float>& f, int32_t row, float speed, float& dA, float& dInner) {
+    const float rho = (float)row / (float)(ARTF_CUDA_MAP_HEIGHT - 1);
+    const float span = 1.f - rho * (1.f - f.inner / f.outer), dspan = rho / f.outer;
+    const float r = f.inner / span, dr = 1.f / span - f.inner * dspan / (span * span);
+    dA = -6.2831853f * speed * speed;
+    dInner = dA * 1.5f * sqrtf(r) * dr;
+}
+
+/* ---- the Nystrom step taken back (lens.inc:165-192) ------------------------------------------------ */
+
+/* The polar part: from the adjoints of (n', v') and of the first stage's a1 (which a crossing reads), adds
+ * to those of (n, v) and the constants. */
+__device__ void polarBack(float a, const RayConst<float>& c, const float* n, const float* v, const float* nNextBar,
+                          const float* vNextBar, const float* a1Extra, float* nBar, float* vBar, ConstBar& g) {
+    const float h = c.step, h2 = h * h, half = h * .5f, eighth = h2 * .125f, halfSq = h2 * .5f;
+    const float sixthSq = h2 * (1.f / 6.f), sixth = h * (1.f / 6.f);
+    float a1[3], midN[3], a2s[3], endN[3], a3[3];
+    accelOf(a, c.big, n, a1);
+    for (int k = 0; k < 3; ++k) midN[k] = n[k] + half * v[k] + eighth * a1[k];
+    accelOf(a, c.big, midN, a2s);
+    for (int k = 0; k < 3; ++k) endN[k] = n[k] + h * v[k] + halfSq * a2s[k];
+    accelOf(a, c.big, endN, a3);
+    float a1Bar[3], a2Bar[3], a3Bar[3], midBar[3] = {0.f, 0.f, 0.f}, endBar[3] = {0.f, 0.f, 0.f}, hBar = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        /* n' = n + h v + h^2/6 (a1 + 2 a2);  v' = v + h/6 (a1 + a3 + 4 a2) */
+        nBar[k] += nNextBar[k];
+        vBar[k] += h * nNextBar[k] + vNextBar[k];
+        a1Bar[k] = sixthSq * nNextBar[k] + sixth * vNextBar[k] + a1Extra[k];
+        a2Bar[k] = 2.f * sixthSq * nNextBar[k] + 4.f * sixth * vNextBar[k];
+        a3Bar[k] = sixth * vNextBar[k];
+        hBar += nNextBar[k] * (v[k] + h * (a1[k] + 2.f * a2s[k]) * (1.f / 3.f)) +
+                vNextBar[k] * (a1[k] + a3[k] + 4.f * a2s[k]) * (1.f / 6.f);
+    }
+    accelBack(a, c.big, endN, a3Bar, endBar, g);
+    for (int k = 0; k < 3; ++k) { /* endN = n + h v + h^2/2 a2 */
+        nBar[k] += endBar[k];
+        vBar[k] += h * endBar[k];
+        a2Bar[k] += halfSq * endBar[k];
+        hBar += endBar[k] * (v[k] + h * a2s[k]);
+    }
+    accelBack(a, c.big, midN, a2Bar, midBar, g);
+    for (int k = 0; k < 3; ++k) { /* midN = n + h/2 v + h^2/8 a1 */
+        nBar[k] += midBar[k];
+        vBar[k] += half * midBar[k];
+        a1Bar[k] += eighth * midBar[k];
+        hBar += midBar[k] * (.5f * v[k] + .25f * h * a1[k]);
+    }
+    accelBack(a, c.big, n, a1Bar, nBar, g);
+    g.step += hBar;
+}
+
+/* The radial part: from the adjoints of (u', w', psi', drag') and of k1, adds to those of (u, w, psi,
+ * drag) and the constants. */
+__device__ void radialBack(float a, const RayConst<float>& c, float u, float w, float drag, float uNextBar,
+                           float wNextBar, float psiNextBar, float dragNextBar, float k1Extra, float& uBar, float& wBar,
+                           float& psiBar, float& dragBar, ConstBar& g) {
+    const float h = c.step, h2 = h * h, half = h * .5f, eighth = h2 * .125f, halfSq = h2 * .5f;
+    const float sixthSq = h2 * (1.f / 6.f), sixth = h * (1.f / 6.f);
+    const float k1 = bendAt(c, u);
+    const float midU = u + half * w + eighth * k1;
+    const float k2 = bendAt(c, midU);
+    const float endU = u + h * w + halfSq * k2;
+    const float k3 = bendAt(c, endU);
+    float hBar = 0.f, midBar = 0.f;
+    if (a != 0.f) {
+        /* drag' = drag(u');  psi' = psi + h/6 (drag + drag' + 4 drag(midU)) */
+        const float uNext = u + h * w + sixthSq * (k1 + (k2 + k2));
+        const float dNext = dragAt(a, a * a, c.xiA, uNext), dMid = dragAt(a, a * a, c.xiA, midU);
+        const float t = psiNextBar * sixth;
+        psiBar += psiNextBar;
+        dragBar += t;
+        hBar += psiNextBar * (drag + dNext + 4.f * dMid) * (1.f / 6.f);
+        dragBack(a, c.xiA, midU, 4.f * t, midBar, g);
+        dragBack(a, c.xiA, uNext, dragNextBar + t, uNextBar, g);
+    }
+    /* u' = u + h w + h^2/6 (k1 + 2 k2);  w' = w + h/6 (k1 + k3 + 4 k2) */
+    uBar += uNextBar;
+    wBar += h * uNextBar + wNextBar;
+    float k1Bar = sixthSq * uNextBar + sixth * wNextBar + k1Extra;
+    float k2Bar = 2.f * sixthSq * uNextBar + 4.f * sixth * wNextBar;
+    const float k3Bar = sixth * wNextBar;
+    hBar += uNextBar * (w + h * (k1 + 2.f * k2) * (1.f / 3.f)) + wNextBar * (k1 + k3 + 4.f * k2) * (1.f / 6.f);
+    float endBar = 0.f; /* endU = u + h w + h^2/2 k2 */
+    bendBack(c, endU, k3Bar, endBar, g);
+    uBar += endBar;
+    wBar += h * endBar;
+    k2Bar += halfSq * endBar;
+    hBar += endBar * (w + h * k2);
+    bendBack(c, midU, k2Bar, midBar, g); /* midU = u + h/2 w + h^2/8 k1 */
+    uBar += midBar;
+    wBar += half * midBar;
+    k1Bar += eighth * midBar;
+    hBar += midBar * (.5f * w + .25f * h * k1);
+    bendBack(c, u, k1Bar, uBar, g);
+    g.step += hBar;
+}
+
+/* The adjoints of one step's start state and of what the crossing and the sky read of its end. */
+struct StepBar {
+    float u, w, n[3], v[3], psi, drag;
+    float k1, a1[3];
+    float nextU, nextN[3], nextPsi, nextDrag;
+};
+
+/* ---- a disc crossing taken back (lens.inc:195-289) ------------------------------------------------- */
+
+__device__ void crossingBack(const AdjointView& v, float rhoScale, const RayConst<float>& c, const RayState<float>& s,
+                             const StepOut<float>& o, const Crossing<float>& x, float throughBefore,
+                             const float* sumBar, float& throughBar, StepBar& b, ConstBar& g) {
+    const Frame<float>& f = v.f;
+    const int32_t mapCount = ARTF_CUDA_MAP_FLOATS, fluidCount = ARTF_CUDA_FLUID_FLOATS;
+    /* the shading's values, as shadeCrossing finds them */
+    const float turn = turnsOf(x.cy, x.cx) + x.psiC * kTurn;
+    const float m2raw = x.cx * x.cx + x.cy * x.cy, m2 = maxX(m2raw, 1e-6f);
+    const float num = x.cx * x.vy - x.cy * x.vx;
+    const float rate = (num / m2 + x.dragC) * kTurn;
+    const float slope = x.wc / x.uc;
+    const float speed2 = x.vx * x.vx + x.vy * x.vy + (x.vz * x.vz + slope * slope);
+    const float invSpeed = 1.f / sqrtf(speed2);
+    const float muRaw = fabsf(x.vz) * invSpeed, mu = maxX(muRaw, .02f);
+    const float slant = f.thickness / 3.f / mu;
+    const float reachA = f.discHeight / maxX(fabsf(x.vz), 1e-5f), reachB = c.step * 1.5f;
+    const float reach = minX(reachA, reachB);
+    const float fluidTime = c.time - f.flow;
+    float clearK[3], alphaK[3], densK[3], litK[3], glow = 0.f, clear = throughBefore;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float t = ((float)k + .5f) * (2.f / 3.f) - 1.f;
+        const float ds = reach * t, uk = x.uc + x.wc * ds, rhoK = (1.f - f.inner * uk) * rhoScale;
+        const bool inside = rhoK > 0.f && rhoK < 1.f;
+        float dens = 0.f, dusty = 0.f;
+        if (inside) {
+            const float rowPos = rhoK * (float)(ARTF_CUDA_MAP_HEIGHT - 1);
+            const float rowFloor = minX(floorf(rowPos), (float)(ARTF_CUDA_MAP_HEIGHT - 2));
+            const int32_t row0 = truncI(rowFloor);
+            const float sp0 = ringSpeedAt(f, v.map, row0), sp1 = ringSpeedAt(f, v.map, row0 + 1);
+            const float turnK = turn + rate * ds;
+            const float d0 = rowAt(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0, turnK - sp0 * c.time);
+            const float d1 = rowAt(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0 + 1, turnK - sp1 * c.time);
+            const float fluidPos = rhoK * (float)(ARTF_CUDA_FLUID_HEIGHT - 1);
+            const float fluidFloor = minX(floorf(fluidPos), (float)(ARTF_CUDA_FLUID_HEIGHT - 2));
+            const int32_t fluidRow = truncI(fluidFloor);
+            const float g0 = rowAt(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow, turnK - sp0 * fluidTime);
+            const float g1 = rowAt(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow + 1, turnK - sp0 * fluidTime);
+            const float gas = g0 + (g1 - g0) * (fluidPos - fluidFloor);
+            const float dustPos = rhoK * (float)(ARTF_CUDA_DUST_HEIGHT - 1);
+            const int32_t dustRow = truncI(minX(floorf(dustPos), (float)(ARTF_CUDA_DUST_HEIGHT - 1)));
+            dusty = rowAt(v.map, mapCount, ARTF_CUDA_DUST_AT, ARTF_CUDA_DUST_WIDTH, dustRow, turnK - sp0 * c.time);
+            const float height = t * (reach / f.discHeight);
+            const float level = maxX(1.f - x.vz * x.vz * (height * height), 0.f);
+            dens = (d0 + (d1 - d0) * (rowPos - rowFloor)) * ((1.f - .1f) + .1f * gas) * level;
+        }
+        const float depth = slant * dens * (1.f + 25.f * dusty);
+        clearK[k] = clear;
+        alphaK[k] = depth / (1.f + depth);
+        densK[k] = dens;
+        litK[k] = 1.f - .97f * dusty;
+        glow = glow + clear * alphaK[k] * (dens * litK[k]);
+        clear = clear * (1.f - alphaK[k]);
+    }
+    const float rhoCenter = (1.f - f.inner * x.uc) * rhoScale;
+    const int32_t rowIndex = truncI(minX(maxX(rhoCenter, 0.f), 1.f) * (float)(ARTF_CUDA_MAP_HEIGHT - 1));
+    float heat = fetch(v.map, clampI(ARTF_CUDA_ROWS_AT + rowIndex + rowIndex + 1, 0, mapCount - 1));
+    const float gives = ringGlowAt(f, v.map, rowIndex);
+    const float light0 = f.gain * glow * gives;
+    float g4 = 1.f;
+    float safeU = 0.f, root = 0.f, lift = 1.f, spinRate = 0.f, sqrtB = 0.f, pShift = 0.f, qShift = 1.f, gShift = 1.f;
+    bool uHeld = false, bHeld = false;
+    if (f.doppler != 0.f) {
+        uHeld = !(x.uc > 1e-4f);
+        safeU = maxX(x.uc, 1e-4f);
+        root = safeU * sqrtf(safeU);
+        lift = 1.f + f.a * root;
+        spinRate = root / lift;
+        const float bRaw = 1.f - 3.f * safeU + (2.f * f.a) * root;
+        bHeld = !(bRaw > 1e-4f);
+        sqrtB = sqrtf(maxX(bRaw, 1e-4f));
+        pShift = c.invEnergy * c.moved;
+        qShift = lift * (1.f - spinRate * c.xi);
+        gShift = 1.f + f.doppler * (sqrtB * pShift / qShift - 1.f);
+        g4 = (gShift * gShift) * (gShift * gShift);
+        heat = heat * gShift;
+    }
+    const int32_t color = truncI(minX(heat * (float)(ARTF_CUDA_COLORS / 2), (float)(ARTF_CUDA_COLORS - 1)));
+    const int32_t at = ARTF_CUDA_COLORS_AT + color + color + color;
+    const float lightBar = sumBar[0] * fetch(v.map, clampI(at, 0, mapCount - 1)) +
+                           sumBar[1] * fetch(v.map, clampI(at + 1, 0, mapCount - 1)) +
+                           sumBar[2] * fetch(v.map, clampI(at + 2, 0, mapCount - 1));
+
+    /* ---- back: light = gain glow gives g^4 ---- */
+    float ucBar = 0.f, wcBar = 0.f, cxBar = 0.f, cyBar = 0.f, vxBar = 0.f, vyBar = 0.f, vzBar = 0.f, psiCBar = 0.f,
+          dragCBar = 0.f;
+    if (f.doppler != 0.f) {
+        const float shiftBar = lightBar * light0 * 4.f * (gShift * gShift * gShift) * f.doppler;
+        const float shift = sqrtB * pShift / qShift;
+        const float sqrtBBar = shiftBar * pShift / qShift, pBar = shiftBar * sqrtB / qShift;
+        const float qBar = -shiftBar * shift / qShift;
+        const float beneathBar = bHeld ? 0.f : sqrtBBar * .5f / sqrtB;
+        float safeUBar = -3.f * beneathBar, rootBar = 2.f * f.a * beneathBar;
+        g.a += 2.f * root * beneathBar;
+        float liftBar = qBar * (1.f - spinRate * c.xi);
+        const float spinRateBar = -qBar * lift * c.xi;
+        g.xi += -qBar * lift * spinRate;
+        rootBar += spinRateBar / lift;
+        liftBar += -spinRateBar * root / (lift * lift);
+        g.a += liftBar * root;
+        rootBar += liftBar * f.a;
+        safeUBar += rootBar * 1.5f * sqrtf(safeU);
+        if (!uHeld) ucBar += safeUBar;
+        g.invEnergy += pBar * c.moved;
+    }
+    const float light0Bar = lightBar * g4;
+    const float glowBar = light0Bar * f.gain * gives;
+    {
+        /* gives = span^q, span = 1 - rho (1 - inner / outer) */
+        const float givesBar = light0Bar * f.gain * glow;
+        const float rho = (float)rowIndex / (float)(ARTF_CUDA_MAP_HEIGHT - 1);
+        const float span = 1.f - rho * (1.f - f.inner / f.outer);
+        g.q += givesBar * gives * logf(span);
+        g.inner += givesBar * f.emissivity * gives / span * (rho / f.outer);
+    }
+    float clearBar = throughBar; /* the transmission after the crossing is the last slice's clear */
+    float reachBar = 0.f, slantBar = 0.f, rateBar = 0.f, turnBar = 0.f;
+    for (int k = 2; k >= 0; --k) {
+        const float t = ((float)k + .5f) * (2.f / 3.f) - 1.f;
+        /* glow += clear alpha dens lit;  clear' = clear (1 - alpha) */
+        const float alphaBar = glowBar * clearK[k] * densK[k] * litK[k] - clearBar * clearK[k];
+        float densBar = glowBar * clearK[k] * alphaK[k] * litK[k];
+        const float litBar = glowBar * clearK[k] * alphaK[k] * densK[k];
+        clearBar = clearBar * (1.f - alphaK[k]) + glowBar * alphaK[k] * densK[k] * litK[k];
+        const float ds = reach * t, uk = x.uc + x.wc * ds, rhoK = (1.f - f.inner * uk) * rhoScale;
+        if (!(rhoK > 0.f && rhoK < 1.f)) continue; /* no gas there: nothing reaches back */
+        const float rowPos = rhoK * (float)(ARTF_CUDA_MAP_HEIGHT - 1);
+        const float rowFloor = minX(floorf(rowPos), (float)(ARTF_CUDA_MAP_HEIGHT - 2)), rowPart = rowPos - rowFloor;
+        const int32_t row0 = truncI(rowFloor);
+        const float sp0 = ringSpeedAt(f, v.map, row0), sp1 = ringSpeedAt(f, v.map, row0 + 1);
+        const float turnK = turn + rate * ds;
+        const float T0 = turnK - sp0 * c.time, T1 = turnK - sp1 * c.time, TF = turnK - sp0 * fluidTime;
+        const float d0 = rowAt(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0, T0);
+        const float d1 = rowAt(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0 + 1, T1);
+        const float fluidPos = rhoK * (float)(ARTF_CUDA_FLUID_HEIGHT - 1);
+        const float fluidFloor = minX(floorf(fluidPos), (float)(ARTF_CUDA_FLUID_HEIGHT - 2));
+        const float fluidPart = fluidPos - fluidFloor;
+        const int32_t fluidRow = truncI(fluidFloor);
+        const float g0 = rowAt(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow, TF);
+        const float g1 = rowAt(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow + 1, TF);
+        const float gas = g0 + (g1 - g0) * fluidPart;
+        const float dens0 = d0 + (d1 - d0) * rowPart, gasFactor = (1.f - .1f) + .1f * gas;
+        const int32_t dustRow =
+            truncI(minX(floorf(rhoK * (float)(ARTF_CUDA_DUST_HEIGHT - 1)), (float)(ARTF_CUDA_DUST_HEIGHT - 1)));
+        const float dusty = rowAt(v.map, mapCount, ARTF_CUDA_DUST_AT, ARTF_CUDA_DUST_WIDTH, dustRow, T0);
+        const float height = t * (reach / f.discHeight);
+        const float levelRaw = 1.f - x.vz * x.vz * (height * height), level = maxX(levelRaw, 0.f);
+        const float dens = dens0 * gasFactor * level, dust25 = 1.f + 25.f * dusty;
+        /* alpha = depth / (1 + depth), depth = slant dens (1 + 25 dusty) */
+        const float depth = slant * dens * dust25;
+        const float depthBar = alphaBar / ((1.f + depth) * (1.f + depth));
+        slantBar += depthBar * dens * dust25;
+        densBar += depthBar * slant * dust25;
+        const float dustyBar = depthBar * slant * dens * 25.f - .97f * litBar;
+        if (levelRaw > 0.f) {
+            const float levelBar = densBar * dens0 * gasFactor;
+            vzBar += levelBar * (-2.f * x.vz * height * height);
+            reachBar += levelBar * (-2.f * x.vz * x.vz * height) * (t / f.discHeight);
+        }
+        const float dens0Bar = densBar * gasFactor * level, gasBar = densBar * dens0 * level * .1f;
+        const float rhoKBar = dens0Bar * (d1 - d0) * (float)(ARTF_CUDA_MAP_HEIGHT - 1) +
+                              gasBar * (g1 - g0) * (float)(ARTF_CUDA_FLUID_HEIGHT - 1);
+        const float T0Bar = dens0Bar * (1.f - rowPart) * rowSlope(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0, T0) +
+                            dustyBar * rowSlope(v.map, mapCount, ARTF_CUDA_DUST_AT, ARTF_CUDA_DUST_WIDTH, dustRow, T0);
+        const float T1Bar = dens0Bar * rowPart * rowSlope(v.map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0 + 1, T1);
+        const float TFBar =
+            gasBar * ((1.f - fluidPart) * rowSlope(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow, TF) +
+                      fluidPart * rowSlope(v.fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow + 1, TF));
+        const float turnKBar = T0Bar + T1Bar + TFBar;
+        {
+            /* T = turnK - speed time: the rings' speeds in a and inner */
+            float dA, dInner;
+            const float sp0Bar = -T0Bar * c.time - TFBar * fluidTime, sp1Bar = -T1Bar * c.time;
+            speedSlopes(f, row0, sp0, dA, dInner);
+            g.a += sp0Bar * dA;
+            g.inner += sp0Bar * dInner;
+            speedSlopes(f, row0 + 1, sp1, dA, dInner);
+            g.a += sp1Bar * dA;
+            g.inner += sp1Bar * dInner;
+        }
+        turnBar += turnKBar;
+        rateBar += turnKBar * ds;
+        /* rhoK = (1 - inner uk) rhoScale, rhoScale = 1 / (1 - inner / outer);  uk = uc + wc ds;  ds = reach t */
+        const float ukBar = -rhoKBar * f.inner * rhoScale;
+        g.inner += rhoKBar * (-uk * rhoScale + (1.f - f.inner * uk) * rhoScale * rhoScale / f.outer);
+        ucBar += ukBar;
+        wcBar += ukBar * ds;
+        reachBar += (turnKBar * rate + ukBar * x.wc) * t;
+    }
+    throughBar = clearBar;
+    /* reach = min(height / max(|vz|, 1e-5), 1.5 step) */
+    if (reachA < reachB) {
+        if (fabsf(x.vz) > 1e-5f) vzBar += -reachBar * reachA / x.vz;
+    } else {
+        g.step += reachBar * 1.5f;
+    }
+    /* slant = thickness / 3 / mu;  mu = max(|vz| / sqrt(speed2), .02);  speed2 = vx^2 + vy^2 + vz^2 + slope^2 */
+    if (muRaw > .02f) {
+        const float muBar = -slantBar * slant / mu;
+        vzBar += muBar * invSpeed * (x.vz < 0.f ? -1.f : 1.f);
+        const float speed2Bar = muBar * fabsf(x.vz) * -.5f * invSpeed / speed2;
+        vxBar += speed2Bar * 2.f * x.vx;
+        vyBar += speed2Bar * 2.f * x.vy;
+        vzBar += speed2Bar * 2.f * x.vz;
+        const float slopeBar = speed2Bar * 2.f * slope; /* slope = wc / uc */
+        wcBar += slopeBar / x.uc;
+        ucBar += -slopeBar * slope / x.uc;
+    }
+    {
+        /* rate = ((cx vy - cy vx) / max(cx^2 + cy^2, 1e-6) + dragC) / 2 pi */
+        const float r = rateBar * kTurn;
+        dragCBar += r;
+        const float numBar = r / m2, m2Bar = -r * num / (m2 * m2);
+        cxBar += numBar * x.vy;
+        vyBar += numBar * x.cx;
+        cyBar += -numBar * x.vx;
+        vxBar += -numBar * x.cy;
+        if (m2raw > 1e-6f) cxBar += m2Bar * 2.f * x.cx, cyBar += m2Bar * 2.f * x.cy;
+    }
+    {
+        /* turn = turns(cy, cx) + psiC / 2 pi */
+        float dy, dx;
+        turnsSlope(x.cy, x.cx, dy, dx);
+        cyBar += turnBar * dy;
+        cxBar += turnBar * dx;
+        psiCBar += turnBar * kTurn;
+    }
+    /* the crossing's state, a second-order step of hu = part h from the step's start */
+    const float h = c.step, hu = x.part * h, hh = hu * hu * .5f;
+    const float huBar = ucBar * (s.w + hu * o.k1) + wcBar * o.k1 + cxBar * (s.v[0] + hu * o.a1[0]) +
+                        cyBar * (s.v[1] + hu * o.a1[1]) + vxBar * o.a1[0] + vyBar * o.a1[1] + vzBar * o.a1[2];
+    b.u += ucBar;
+    b.w += ucBar * hu + wcBar;
+    b.k1 += ucBar * hh + wcBar * hu;
+    b.n[0] += cxBar;
+    b.n[1] += cyBar;
+    b.v[0] += cxBar * hu + vxBar;
+    b.v[1] += cyBar * hu + vyBar;
+    b.v[2] += vzBar;
+    b.a1[0] += cxBar * hh + vxBar * hu;
+    b.a1[1] += cyBar * hh + vyBar * hu;
+    b.a1[2] += vzBar * hu;
+    b.psi += psiCBar * (1.f - x.part);
+    b.nextPsi += psiCBar * x.part;
+    b.drag += dragCBar * (1.f - x.part);
+    b.nextDrag += dragCBar * x.part;
+    g.step += huBar * x.part;
+    /* part = nz / (nz - nz') */
+    const float partBar = huBar * h + psiCBar * (o.next.psi - s.psi) + dragCBar * (o.next.drag - s.drag);
+    const float den = s.n[2] - o.next.n[2];
+    b.n[2] += -partBar * o.next.n[2] / (den * den);
+    b.nextN[2] += partBar * s.n[2] / (den * den);
+}
+
+/* ---- the escape taken back (lens.inc:316-346) ------------------------------------------------------ */
+
+__device__ void skyBack(const AdjointView& v, const RayConst<float>& c, const RayState<float>& s,
+                        const RayState<float>& next, float through, const float* sumBar, float& throughBar,
+                        StepBar& b, ConstBar& g) {
+    const Frame<float>& f = v.f;
+    const float part = s.u / (s.u - next.u);
+    float away[3];
+    for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (next.n[k] - s.n[k]);
+    const float awayPsi = s.psi + part * (next.psi - s.psi);
+    const float len2raw = away[0] * away[0] + away[1] * away[1] + away[2] * away[2];
+    const float invA = 1.f / sqrtf(maxX(len2raw, 1e-12f));
+    const float psiT = awayPsi * kTurn;
+    const float sine = sineOf(psiT), cosine = sineOf(psiT + .25f);
+    const float x = away[0] * invA, y = away[1] * invA, m = away[2] * invA;
+    const float dir[3] = {x * cosine - y * sine, x * sine + y * cosine, m};
+    float rgb[3] = {0.f, 0.f, 0.f};
+    starLayer(dir, 90.f, 26, .1f, 1.6f, rgb);
+    starLayer(dir, 240.f, 70, .17f, .22f, rgb);
+    const float skyTurn = turnsOf(dir[1], dir[0]);
+    const float heightPos = (dir[2] * .5f + .5f) * (float)(ARTF_CUDA_SKY_HEIGHT - 1);
+    const float skyFloor = minX(floorf(heightPos), (float)(ARTF_CUDA_SKY_HEIGHT - 2)), skyPart = heightPos - skyFloor;
+    const int32_t skyRow = truncI(skyFloor);
+    const float s0 = rowAt(v.map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH, skyRow, skyTurn);
+    const float s1 = rowAt(v.map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH, skyRow + 1, skyTurn);
+    const float dust = s0 + (s1 - s0) * skyPart;
+    rgb[0] = rgb[0] + dust * .92f;
+    rgb[1] = rgb[1] + dust * .86f;
+    rgb[2] = rgb[2] + dust;
+    float g1 = 1.f, g14 = 1.f;
+    if (f.doppler != 0.f) {
+        g1 = 1.f + f.doppler * (c.invEnergy * c.moved - 1.f);
+        g14 = (g1 * g1) * (g1 * g1);
+    }
+    const float shown = through * f.stars * g14;
+    /* back */
+    const float rgbBar[3] = {sumBar[0] * shown, sumBar[1] * shown, sumBar[2] * shown};
+    const float shownBar = sumBar[0] * rgb[0] + sumBar[1] * rgb[1] + sumBar[2] * rgb[2];
+    throughBar += shownBar * f.stars * g14;
+    if (f.doppler != 0.f) g.invEnergy += shownBar * through * f.stars * 4.f * (g1 * g1 * g1) * f.doppler * c.moved;
+    float dirBar[3] = {0.f, 0.f, 0.f};
+    {
+        /* the dust: rows by height, columns by the turn */
+        const float dustBar = rgbBar[0] * .92f + rgbBar[1] * .86f + rgbBar[2];
+        dirBar[2] += dustBar * (s1 - s0) * .5f * (float)(ARTF_CUDA_SKY_HEIGHT - 1);
+        const float turnBar =
+            dustBar * ((1.f - skyPart) * rowSlope(v.map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH,
+                                                  skyRow, skyTurn) +
+                       skyPart * rowSlope(v.map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH,
+                                          skyRow + 1, skyTurn));
+        float dy, dx;
+        turnsSlope(dir[1], dir[0], dy, dx);
+        dirBar[1] += turnBar * dy;
+        dirBar[0] += turnBar * dx;
+    }
+    /* the two star layers (lens.inc:69-86): light = max(1 - d^2 / size^2, 0)^2 gain */
+    const float layer[2][4] = {{90.f, 26.f, .1f, 1.6f}, {240.f, 70.f, .17f, .22f}};
+    for (int l = 0; l < 2; ++l) {
+        const float cells = layer[l][0], size = layer[l][2], gain = layer[l][3];
+        const float px = dir[0] * cells, py = dir[1] * cells, pz = dir[2] * cells;
+        const float cx = floorf(px), cy = floorf(py), cz = floorf(pz);
+        const uint32_t hash = cubeHash((uint32_t)truncI(cx), (uint32_t)truncI(cy), (uint32_t)truncI(cz));
+        if (!((int32_t)layer[l][1] > (int32_t)(hash & 255u))) continue;
+        const float inv255 = 1.f / 255.f;
+        const float e[3] = {px - cx - (float)((hash >> 8) & 255u) * inv255, py - cy - (float)((hash >> 16) & 255u) * inv255,
+                            pz - cz - (float)((hash >> 24) & 255u) * inv255};
+        const float base = 1.f - (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * (1.f / (size * size));
+        if (!(base > 0.f)) continue;
+        const float warm = (float)((hash >> 3) & 255u) * inv255;
+        const float lightBar = rgbBar[0] * (.75f + warm * .25f) + rgbBar[1] * .82f + rgbBar[2] * (1.f - warm * .45f);
+        const float d2Bar = -lightBar * 2.f * base * gain / (size * size);
+        for (int k = 0; k < 3; ++k) dirBar[k] += d2Bar * 2.f * e[k] * cells;
+    }
+    /* dir = (x cos - y sin, x sin + y cos, m), (x, y, m) = away / |away|, the angle psi / 2 pi */
+    const float xBar = dirBar[0] * cosine + dirBar[1] * sine, yBar = dirBar[1] * cosine - dirBar[0] * sine;
+    const float psiTBar = (dirBar[1] * x - dirBar[0] * y) * sineSlope(psiT) + (dirBar[0] * x + dirBar[1] * y) * sineSlope(psiT + .25f);
+    const float awayPsiBar = psiTBar * kTurn;
+    float awayBar[3] = {xBar * invA, yBar * invA, dirBar[2] * invA};
+    if (len2raw > 1e-12f) {
+        const float k = -(xBar * away[0] + yBar * away[1] + dirBar[2] * away[2]) * invA * invA * invA;
+        for (int i = 0; i < 3; ++i) awayBar[i] += k * away[i];
+    }
+    /* away = n + part (n' - n);  awayPsi = psi + part (psi' - psi);  part = u / (u - u') */
+    float partBar = awayPsiBar * (next.psi - s.psi);
+    for (int k = 0; k < 3; ++k) {
+        b.n[k] += awayBar[k] * (1.f - part);
+        b.nextN[k] += awayBar[k] * part;
+        partBar += awayBar[k] * (next.n[k] - s.n[k]);
+    }
+    b.psi += awayPsiBar * (1.f - part);
+    b.nextPsi += awayPsiBar * part;
+    const float den = s.u - next.u;
+    b.u += -partBar * next.u / (den * den);
+    b.nextU += partBar * s.u / (den * den);
+}
+
+/* ---- the ray's set-up taken back (lens.inc:101-152), and onto theta ---------------------------------- */
+
+__device__ void startBack(const AdjointView& v, float nx, float ny, const RayConst<float>& c, const StepBar& x0,
+                          ConstBar g, float* grad) {
+    const Frame<float>& f = v.f;
+    float d[3];
+    for (int k = 0; k < 3; ++k) d[k] = f.forward[k] + nx * f.right[k] + ny * f.up[k];
+    const float inv = 1.f / sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const float e[3] = {d[0] * inv, d[1] * inv, d[2] * inv};
+    const float a = f.a, rho = f.place[0], rootDelta = f.place[1], u0 = f.place[2], mu0 = f.place[3];
+    const float iE = c.invEnergy, xi = c.xi;
+    const float xa = f.metric[3] * e[2] * iE, ac = rho * e[1] * iE;
+    const float eta = ac * ac + mu0 * mu0 * (xa * xa - a * a);
+    const float P = -u0 * u0 * rootDelta * rho;
+    float fieldBar[ARTF_CUDA_GRAD_FIELDS];
+#pragma unroll
+    for (int k = 0; k < ARTF_CUDA_GRAD_FIELDS; ++k) fieldBar[k] = 0.f;
+    /* the first state: u = u0, w = P e_x / E, n = er, v = ac etheta + xa ephi, drag = drag(u0) */
+    float u0Bar = x0.u, acBar = 0.f, xaBar = 0.f, eBar[3] = {0.f, 0.f, 0.f}, iEBar = g.invEnergy, xiBar = g.xi;
+    if (a != 0.f) dragBack(a, c.xiA, u0, x0.drag, u0Bar, g);
+    for (int k = 0; k < 3; ++k) {
+        fieldBar[17 + k] += x0.n[k];
+        fieldBar[20 + k] += x0.v[k] * ac;
+        fieldBar[23 + k] += x0.v[k] * xa;
+        acBar += x0.v[k] * f.etheta[k];
+        xaBar += x0.v[k] * f.ephi[k];
+    }
+    const float PBar = x0.w * e[0] * iE;
+    eBar[0] += x0.w * P * iE;
+    iEBar += x0.w * P * e[0];
+    u0Bar += PBar * (-2.f * u0 * rootDelta * rho);
+    const float rootDeltaBar = PBar * (-u0 * u0 * rho);
+    float rhoBar = PBar * (-u0 * u0 * rootDelta);
+    /* xiA = xi a;  uC = -2 a^2 eta;  uB = 3 (eta + (xi - a)^2);  uA = a^2 - K;  K = eta + xi^2 */
+    xiBar += g.xiA * a;
+    g.a += g.xiA * xi;
+    float etaBar = -2.f * a * a * g.uC + 3.f * g.uB;
+    g.a += -4.f * a * eta * g.uC;
+    const float offBar = 6.f * (xi - a) * g.uB;
+    xiBar += offBar;
+    g.a += -offBar + 2.f * a * g.uA;
+    float bigBar = g.big - g.uA;
+    if (c.big > 4.f) bigBar += g.step * (-.5f * c.step / c.big); /* step = C / sqrt(max(K, 4)) */
+    etaBar += bigBar;
+    xiBar += 2.f * xi * bigBar;
+    /* eta = ac^2 + mu0^2 (xa^2 - a^2) */
+    acBar += 2.f * ac * etaBar;
+    const float mu0Bar = 2.f * mu0 * (xa * xa - a * a) * etaBar;
+    xaBar += 2.f * mu0 * mu0 * xa * etaBar;
+    g.a += -2.f * a * mu0 * mu0 * etaBar;
+    /* ac = rho e_y / E;  xa = m3 e_z / E;  xi = -m2 e_z / E;  E = m0 - m1 e_z */
+    rhoBar += acBar * e[1] * iE;
+    eBar[1] += acBar * rho * iE;
+    iEBar += acBar * rho * e[1] + xaBar * f.metric[3] * e[2] - xiBar * f.metric[2] * e[2];
+    fieldBar[12] += xaBar * e[2] * iE;
+    fieldBar[11] += -xiBar * e[2] * iE;
+    eBar[2] += (xaBar * f.metric[3] - xiBar * f.metric[2]) * iE;
+    const float EBar = -iEBar * iE * iE;
+    fieldBar[9] += EBar;
+    fieldBar[10] += -EBar * e[2];
+    eBar[2] += -EBar * f.metric[1];
+    /* e = d / |d|, d = forward + nx right + ny up */
+    const float dot = (eBar[0] * d[0] + eBar[1] * d[1] + eBar[2] * d[2]) * inv * inv * inv;
+    for (int k = 0; k < 3; ++k) {
+        const float dBar = eBar[k] * inv - dot * d[k];
+        fieldBar[k] += dBar;
+        fieldBar[3 + k] += dBar * nx;
+        fieldBar[6 + k] += dBar * ny;
+    }
+    fieldBar[13] += rhoBar;
+    fieldBar[14] += rootDeltaBar;
+    fieldBar[15] += u0Bar;
+    fieldBar[16] += mu0Bar;
+    fieldBar[26] += g.a;
+    fieldBar[27] += g.inner;
+#pragma unroll
+    for (int k = 0; k < ARTF_CUDA_GRAD_FIELDS; ++k)
+#pragma unroll
+        for (int q = 0; q < 5; ++q) grad[q] += fieldBar[k] * v.jacobian[k][q];
+    grad[3] += g.q;
+}
+
+/* ---- the kernels -------------------------------------------------------------------------------- */
+
+struct Kept {
+    RayState<float> s;
+    float through; /* the disc's transmission before this step's crossing */
+};
+
+struct AdjointLaunch {
+    const AdjointView* views;
+    float* partials; /* 8 floats a block: the loss, the five gradient components, two spare */
+    unsigned long long* counters;
+    int blocksPerView, K;
+};
+
+/* One step from s, with its crossing's shading. */
+__device__ __forceinline__ void stepOnce(const AdjointView& v, float rhoScale, const RayConst<float>& c,
+                                         const RayState<float>& s, StepOut<float>& o, float& through, float* sum,
+                                         unsigned& crossings) {
+    nystromStep(v.f.a, c, s, o);
+    Crossing<float> x;
+    if (crossingOf(v.f, rhoScale, c, s, o, x)) {
+        float turn;
+        shadeCrossing(v.f, rhoScale, v.map, v.fluid, c, x, through, sum, &turn);
+        ++crossings;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L) {
+    __shared__ AdjointView v;
+    {
+        const int4* src = reinterpret_cast<const int4*>(L.views + blockIdx.y);
+        int4* dst = reinterpret_cast<int4*>(&v);
+        for (int k = threadIdx.x; k < (int)(sizeof(AdjointView) / 16); k += kThreads) dst[k] = src[k];
+    }
+    __syncthreads();
+    const Frame<float>& f = v.f;
+    const int i = (int)(blockIdx.x * kThreads + threadIdx.x);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    Tally tally;
+    if (i < v.pixels) {
+        const int px = i % f.width, py = i / f.width;
+        float nx, ny, moment;
+        samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
+        RayConst<float> c;
+        RayState<float> s;
+        rayStart(f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
+        const float a = f.a;
+        if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
+        const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
+        const int K = L.K;
+        Kept ring[kMaxK + 1];
+        Kept checkpoint[kMaxSegments];
+        /* forward: the segment's states, and each segment's first */
+        float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
+        int steps = 0;
+        unsigned crossings = 0;
+        bool escaped = false;
+        RayState<float> end = s;
+        for (int step = 0; step < kMaxSteps; ++step) {
+            if (step % K == 0) checkpoint[step / K] = Kept{s, through};
+            ring[step % K] = Kept{s, through};
+            StepOut<float> o;
+            stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
+            ++steps;
+            end = o.next;
+            if (0.f > o.next.u) {
+                const float part = s.u / (s.u - o.next.u);
+                float away[3], dir[3];
+                for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
+                skyDirection(away, s.psi + part * (o.next.psi - s.psi), dir);
+                if (f.stars > 0.f) shadeSky(f, v.map, c, dir, through, sum);
+                escaped = true;
+                break;
+            }
+            if (o.next.u > f.uHorizon || !(through > .004f)) break;
+            s = o.next;
+        }
+        const int lastFirst = ((steps - 1) / K) * K;
+        ring[steps - lastFirst] = Kept{end, through};
+        /* the loss, and its adjoint in the radiance */
+        const float4 want = v.target[i];
+        const float diff[3] = {sum[0] - want.x, sum[1] - want.y, sum[2] - want.z};
+        acc[0] = (diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]) * v.lossScale;
+        const float sumBar[3] = {2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale, 2.f * diff[2] * v.lossScale};
+        if (v.hdr) v.hdr[i] = make_float4(sum[0], sum[1], sum[2], 0.f);
+        const float throughEnd = through;
+        /* back, a segment at a time */
+        StepBar next;
+        memset(&next, 0, sizeof next);
+        ConstBar g;
+        memset(&g, 0, sizeof g);
+        float throughBar = 0.f;
+        for (int first = lastFirst; first >= 0; first -= K) {
+            const int last = min(first + K, steps); /* steps first .. last - 1 */
+            if (first != lastFirst) {
+                RayState<float> r = checkpoint[first / K].s;
+                float t = checkpoint[first / K].through, junk[3] = {0.f, 0.f, 0.f};
+                unsigned n = 0;
+                for (int step = first; step < last; ++step) {
+                    ring[step - first] = Kept{r, t};
+                    StepOut<float> o;
+                    stepOnce(v, rhoScale, c, r, o, t, junk, n);
+                    r = o.next;
+                }
+                ring[last - first] = Kept{r, t};
+            }
+            for (int step = last - 1; step >= first; --step) {
+                const Kept k = ring[step - first];
+                StepOut<float> o;
+                o.next = ring[step - first + 1].s;
+                o.k1 = bendAt(c, k.s.u);
+                accelOf(a, c.big, k.s.n, o.a1);
+                StepBar b;
+                memset(&b, 0, sizeof b);
+                b.nextU = next.u;
+                for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
+                b.nextPsi = next.psi;
+                b.nextDrag = next.drag;
+                if (escaped && step == steps - 1 && f.stars > 0.f)
+                    skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
+                Crossing<float> x;
+                if (crossingOf(f, rhoScale, c, k.s, o, x))
+                    crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
+                radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w, b.psi,
+                           b.drag, g);
+                polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
+                next = b;
+            }
+        }
+        startBack(v, nx, ny, c, next, g, acc + 1);
+        if (v.pixelGrads)
+            for (int q = 0; q < 5; ++q) v.pixelGrads[(size_t)i * 5 + q] = acc[1 + q];
+        tally.rays = 1, tally.steps = (unsigned)steps, tally.crossings = crossings, tally.escapes = escaped;
+    }
+    flushTally(tally, L.counters);
+    /* the block's sums, in a fixed order */
+    __shared__ float warpSums[kThreads / 32][6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float s = acc[k];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
+        if ((threadIdx.x & 31) == 0) warpSums[threadIdx.x >> 5][k] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        float s = 0.f;
+        if (threadIdx.x < 6)
+            for (int w = 0; w < kThreads / 32; ++w) s += warpSums[w][threadIdx.x];
+        L.partials[((size_t)blockIdx.y * L.blocksPerView + blockIdx.x) * 8 + threadIdx.x] = s;
+    }
+}
+
+/* One block a view: its blocks' sums added in double, in a fixed order. */
+__global__ void __launch_bounds__(256) adjointSums(const float* partials, int blocksPerView, double* results) {
+    __shared__ double part[256];
+    const float* mine = partials + (size_t)blockIdx.x * blocksPerView * 8;
+    for (int k = 0; k < 6; ++k) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < blocksPerView; b += 256) s += (double)mine[(size_t)b * 8 + k];
+        part[threadIdx.x] = s;
+        __syncthreads();
+        for (int width = 128; width > 0; width >>= 1) {
+            if ((int)threadIdx.x < width) part[threadIdx.x] += part[threadIdx.x + width];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) results[(size_t)blockIdx.x * 8 + k] = part[0];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+size_t adjointViewBytes() { return sizeof(AdjointView); }
+
+int adjointBlocks(int pixels) { return (pixels + kThreads - 1) / kThreads; }
+
+void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* jacobian, double emissivity,
+                     const float* map, const float* fluid, const float* target, float* hdr, float* pixelGrads) {
+    AdjointView v;
+    memset(&v, 0, sizeof v);
+    v.f.load(frame, frame);
+    v.f.analyticTables = 1;
+    v.f.emissivity = (float)emissivity;
+    v.h = frame;
+    for (int k = 0; k < ARTF_CUDA_GRAD_FIELDS; ++k)
+        for (int q = 0; q < 5; ++q) v.jacobian[k][q] = (float)jacobian[k * 5 + q];
+    v.map = map;
+    v.fluid = fluid;
+    v.target = (const float4*)target;
+    v.hdr = (float4*)hdr;
+    v.pixelGrads = pixelGrads;
+    v.pixels = (int)(frame.size[0] * frame.size[1]);
+    v.lossScale = 1.f / (3.f * (float)v.pixels);
+    memcpy(slot, &v, sizeof v);
+}
+
+cudaError_t launchAdjoint(const void* table, int count, int pixels, int K, unsigned long long* counters,
+                          float* partials, double* results, cudaStream_t stream) {
+    AdjointLaunch L;
+    L.views = (const AdjointView*)table;
+    L.partials = partials;
+    L.counters = counters;
+    L.blocksPerView = adjointBlocks(pixels);
+    L.K = K;
+    adjointPixels<<<dim3((unsigned)L.blocksPerView, (unsigned)count), kThreads, 0, stream>>>(L);
+    adjointSums<<<count, 256, 0, stream>>>(partials, L.blocksPerView, results);
+    return cudaGetLastError();
+}
+
+}  // namespace artf

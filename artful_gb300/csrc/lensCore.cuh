@@ -127,6 +127,11 @@ template <typename R> struct Frame {
     R inner, outer, time, thickness, gain, doppler, stars;
     R pixelX, pixelY, share; /* 2/width, 2/height, 1/(rays a pixel) */
     int32_t width, height, side;
+    /* The differentiated traces evaluate the two map tables that depend on the scene's parameters (the
+     * rings' orbit speed and their glow, (r / inner)^-q) from their formulas, so that the parameters'
+     * derivatives flow through them; every other trace reads the tables. */
+    int32_t analyticTables;
+    R emissivity;
 
     template <typename F> ARTF_HD void load(const F& f, const ArtfCudaHoleFrame& sizes) {
         for (int c = 0; c < 3; ++c) {
@@ -140,8 +145,35 @@ template <typename R> struct Frame {
         gain = R(f.look[0]), doppler = R(f.look[1]), stars = R(f.look[2]);
         pixelX = R(f.image[1]), pixelY = R(f.image[2]), share = R(f.image[3]);
         width = (int32_t)sizes.size[0], height = (int32_t)sizes.size[1], side = (int32_t)sizes.size[2];
+        analyticTables = 0;
+        emissivity = R(0);
     }
 };
+
+ARTF_HD float expR(float x) { return expf(x); }
+ARTF_HD double expR(double x) { return exp(x); }
+ARTF_HD float logR(float x) { return logf(x); }
+ARTF_HD double logR(double x) { return log(x); }
+
+/* The rings' orbit speed at a map row (hole.c:186-191 setRings, rows even in 1/r). */
+template <typename R> ARTF_HD R ringSpeedAt(const Frame<R>& f, const float* map, int32_t row) {
+    if (f.analyticTables) {
+        const R rho = R((float)row / (float)(ARTF_CUDA_MAP_HEIGHT - 1));
+        const R r = divR(f.inner, R(1) - rho * (R(1) - divR(f.inner, f.outer)));
+        return recipR(KF(6.2831853) * (r * rootR(r) + f.a));
+    }
+    return R(fetch(map, clampI(ARTF_CUDA_ROWS_AT + row + row, 0, ARTF_CUDA_MAP_FLOATS - 1)));
+}
+
+/* The rings' glow at a map row: (r / inner)^-q of the synthetic disc. */
+template <typename R> ARTF_HD R ringGlowAt(const Frame<R>& f, const float* map, int32_t row) {
+    if (f.analyticTables) {
+        const R rho = R((float)row / (float)(ARTF_CUDA_MAP_HEIGHT - 1));
+        const R span = R(1) - rho * (R(1) - divR(f.inner, f.outer)); /* inner / r */
+        return expR(f.emissivity * logR(span));
+    }
+    return R(fetch(map, clampI(ARTF_CUDA_GLOW_AT + row, 0, ARTF_CUDA_MAP_FLOATS - 1)));
+}
 
 /* ---- per ray ------------------------------------------------------------------------------------ */
 
@@ -398,8 +430,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
         const R rowFloor = minX(floorR(rowPos), R(ARTF_CUDA_MAP_HEIGHT - 2));
         const R rowPart = rowPos - rowFloor;
         const int32_t row0 = truncI(rowFloor), row1 = row0 + 1;
-        const R speed0 = R(fetch(map, clampI(ARTF_CUDA_ROWS_AT + row0 + row0, 0, mapCount - 1)));
-        const R speed1 = R(fetch(map, clampI(ARTF_CUDA_ROWS_AT + row1 + row1, 0, mapCount - 1)));
+        const R speed0 = ringSpeedAt(f, map, row0), speed1 = ringSpeedAt(f, map, row1);
         const R turnK = turn + (inside ? rate * ds : R(0));
         const R d0 = rowAt(map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0, turnK - speed0 * c.time);
         const R d1 = rowAt(map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row1, turnK - speed1 * c.time);
@@ -433,7 +464,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
     const R rhoSafe = minX(maxX(rhoCenter, R(0)), R(1));
     const int32_t rowIndex = truncI(rhoSafe * R(ARTF_CUDA_MAP_HEIGHT - 1));
     R heat = R(fetch(map, clampI(ARTF_CUDA_ROWS_AT + rowIndex + rowIndex + 1, 0, mapCount - 1)));
-    const R gives = R(fetch(map, clampI(ARTF_CUDA_GLOW_AT + rowIndex, 0, mapCount - 1)));
+    const R gives = ringGlowAt(f, map, rowIndex);
     R light = f.gain * glow * gives;
     if (f.doppler != R(0)) {
         const R safeU = maxX(x.uc, KF(1e-4));

@@ -329,6 +329,63 @@ int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const Artf
                        const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                        const ArtfCudaTraceOptions* options, float* hostHdr, ArtfCudaTraceStats* stats);
 
+/* ---- gradients of an image loss (no reference counterpart) ---------------------------------------- */
+
+/* A scene by its five physical parameters, theta = (spin a, inclination i in radians from the axis,
+ * inner disc radius as a multiple of the ISCO, emissivity index q, observer distance r_obs), the eye at
+ * r_obs (0, cos i, sin i) looking at the hole with +y up, the hole's axis +y, one ray at each pixel's
+ * centre, and the synthetic disc (artfCudaSynthMap) of emissivity r^-q.  The remaining fields hold
+ * fixed. */
+typedef struct ArtfCudaHoleParams {
+    double spin, inclination, innerScale, emissivity, distance;
+    double fovY, outer, height, thickness, gain, doppler, stars, time;
+    uint64_t seed;
+} ArtfCudaHoleParams;
+
+/* The frame fields the parameters reach: forward, right, up (3 each), metric (4), place (4), er,
+ * etheta, ephi (3 each), the spin, the inner radius. */
+#define ARTF_CUDA_GRAD_FIELDS 28
+
+/* The scene's camera and description; its FP32 and FP64 frames and the Jacobian of the frame fields in
+ * theta (ARTF_CUDA_GRAD_FIELDS x 5, row-major: central differences of the FP64 frame); its map.  Any
+ * output may be NULL.  The inner radius is used as given (not clamped). */
+int artfCudaHoleParamsScene(const ArtfCudaHoleParams* params, ArtfCudaCamera* camera, ArtfCudaBlackHoleDesc* desc);
+int artfCudaHoleParamsFrames(const ArtfCudaHoleParams* params, int width, int height, ArtfCudaHoleFrame* frame,
+                             ArtfCudaHoleFrame64* frame64, double* jacobian);
+int artfCudaHoleParamsMap(const ArtfCudaHoleParams* params, float* map);
+
+/* The FP64 forward-mode reference: for each pixel and colour channel, its radiance and the radiance's
+ * five derivatives in theta, into `out` (device, width * height * 3 * 6 doubles).  map and fluid: device
+ * pointers (NULL: the context's).  Synchronous. */
+int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* params, const ArtfCudaHoleFrame* frame,
+                         const ArtfCudaHoleFrame64* frame64, const double* jacobian, const float* map,
+                         const float* fluid, double* out);
+
+#define ARTF_CUDA_ADJOINT_MIN_CHECKPOINT 8
+#define ARTF_CUDA_ADJOINT_MAX_CHECKPOINT 64
+#define ARTF_CUDA_ADJOINT_MAX_VIEWS 1024
+
+/* A view's loss, L = sum over pixels and colour channels of (radiance - target)^2 / (3 * pixels), and
+ * its gradient in theta = (spin, inclination, innerScale, emissivity, distance). */
+typedef struct ArtfCudaAdjointResult {
+    double loss;
+    double grad[5];
+} ArtfCudaAdjointResult;
+
+/* The adjoint: reverse-mode derivatives of the FP32 trace, checkpointing the ray's state every
+ * `checkpointEvery` steps (ARTF_CUDA_ADJOINT_MIN_CHECKPOINT .. ARTF_CUDA_ADJOINT_MAX_CHECKPOINT) and
+ * recomputing in between.  `count` views (params[0 .. count - 1]) of one size, one ray at each pixel's
+ * centre, in one launch.  The rings' orbit speed and glow come from their formulas; the map's other
+ * tables (gas, dust, sky, colours) and the fluid are shared by the views: device pointers (NULL: the
+ * context's).  targets: device, count * width * height float4 (linear RGB, the fourth unused).  hdr:
+ * device, the same size, or NULL: the radiance the adjoint's forward pass found.  pixelGrads: device,
+ * count * width * height * 5 floats, or NULL: each pixel's share of its view's gradient.  results: host,
+ * count entries.  stats: rays, steps, crossings, escapes of the forward pass, and the launch's device
+ * time.  Synchronous. */
+int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
+                        const float* map, const float* fluid, const float* targets, int checkpointEvery, float* hdr,
+                        float* pixelGrads, ArtfCudaAdjointResult* results, ArtfCudaTraceStats* stats);
+
 /* ---- measurement ------------------------------------------------------------------------------- */
 
 /* The device's FP32 and FP64 fused multiply-add throughput, measured (flop/s, a multiply-add two):
