@@ -529,7 +529,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
         return fail(ARTF_CUDA_EINVAL, "checkpoint interval %d (%d .. %d)", checkpointEvery,
                     ARTF_CUDA_ADJOINT_MIN_CHECKPOINT, ARTF_CUDA_ADJOINT_MAX_CHECKPOINT);
     if ((!map && !ctx->mapHeld) || (!fluid && !ctx->fluidHeld)) return fail(ARTF_CUDA_EINVAL, "no map or fluid");
-    const int pixels = width * height, blocks = artf::adjointBlocks(pixels);
+    const int pixels = width * height, blocks = artf::adjointTiles(width, height);
     if ((status = reserveAdjoint(ctx, count, blocks))) return status;
     /* (the staging is free: every call ends synchronised) */
     const size_t slot = artf::adjointViewBytes();
@@ -549,7 +549,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
             cudaMemcpyAsync(ctx->adjTable, ctx->adjStage, slot * count, cudaMemcpyHostToDevice, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-    const cudaError_t e = artf::launchAdjoint(ctx->adjTable, count, pixels, checkpointEvery, ctx->counters,
+    const cudaError_t e = artf::launchAdjoint(ctx->adjTable, count, width, height, checkpointEvery, ctx->counters,
                                               ctx->adjPartials, ctx->adjResults, ctx->stream);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "adjoint launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));

@@ -18,9 +18,10 @@
  * derivative (which texel or star cell, the 0.004 opacity cut-off, the step cap) contribute none: the
  * pathwise derivative.
  *
- * Work layout: a view table in device memory (one entry a view, copied to shared memory by each block),
- * blocks of 128 threads, grid (blocks a view, views).  Each block writes its six sums; a second kernel
- * adds them in a fixed order, in double, so the result does not depend on scheduling. */
+ * Work layout: a view table in device memory; grid (blocks of four 8 x 4 tiles, views), each block
+ * copying its view's entry to shared memory, each warp tracing one tile.  Each tile's six sums go to the
+ * tile's own slot; a second kernel adds them in a fixed order, in double, so the result does not depend
+ * on scheduling. */
 #include "lensKernel.cuh"
 #include "lensTangent.h"
 
@@ -679,9 +680,9 @@ struct Kept {
 
 struct AdjointLaunch {
     const AdjointView* views;
-    float* partials; /* 8 floats a block: the loss, the five gradient components, two spare */
+    float* partials; /* 8 floats a tile: the loss, the five gradient components, two unused */
     unsigned long long* counters;
-    int blocksPerView, K;
+    int tilesX, tilesPerView, totalTiles, K;
 };
 
 /* One step from s, with its crossing's shading. */
@@ -697,6 +698,114 @@ __device__ __forceinline__ void stepOnce(const AdjointView& v, float rhoScale, c
     }
 }
 
+/* Pixel i's ray: forward with checkpoints, the loss, back; adds the loss and its gradient to acc. */
+__device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py, int K, float* acc, Tally& tally) {
+    const Frame<float>& f = v.f;
+    const int i = py * f.width + px;
+    float nx, ny, moment;
+    samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
+    RayConst<float> c;
+    RayState<float> s;
+    rayStart(f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
+    const float a = f.a;
+    if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
+    const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
+    Kept ring[kMaxK + 1];
+    Kept checkpoint[kMaxSegments];
+    /* forward: the segment's states, and each segment's first */
+    float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
+    int steps = 0;
+    unsigned crossings = 0;
+    bool escaped = false;
+    RayState<float> end = s;
+    for (int step = 0; step < kMaxSteps; ++step) {
+        if (step % K == 0) checkpoint[step / K] = Kept{s, through};
+        ring[step % K] = Kept{s, through};
+        StepOut<float> o;
+        stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
+        ++steps;
+        end = o.next;
+        if (0.f > o.next.u) {
+            const float part = s.u / (s.u - o.next.u);
+            float away[3], dir[3];
+            for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
+            skyDirection(away, s.psi + part * (o.next.psi - s.psi), dir);
+            if (f.stars > 0.f) shadeSky(f, v.map, c, dir, through, sum);
+            escaped = true;
+            break;
+        }
+        if (o.next.u > f.uHorizon || !(through > .004f)) break;
+        s = o.next;
+    }
+    const int lastFirst = ((steps - 1) / K) * K;
+    /* the loss, and its adjoint in the radiance */
+    const float4 want = v.target[i];
+    const float diff[3] = {sum[0] - want.x, sum[1] - want.y, sum[2] - want.z};
+    acc[0] += (diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]) * v.lossScale;
+    const float sumBar[3] = {2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale, 2.f * diff[2] * v.lossScale};
+    if (v.hdr) v.hdr[i] = make_float4(sum[0], sum[1], sum[2], 0.f);
+    const float throughEnd = through;
+    /* back, a segment at a time */
+    StepBar next;
+    memset(&next, 0, sizeof next);
+    ConstBar g;
+    memset(&g, 0, sizeof g);
+    float throughBar = 0.f;
+    for (int first = lastFirst; first >= 0; first -= K) {
+        const int last = min(first + K, steps); /* steps first .. last - 1 */
+        RayState<float> after = end;            /* the state at the segment's end */
+        if (first != lastFirst) {
+            RayState<float> r = checkpoint[first / K].s;
+            float t = checkpoint[first / K].through, junk[3] = {0.f, 0.f, 0.f};
+            unsigned n = 0;
+            for (int step = first; step < last; ++step) {
+                ring[step - first] = Kept{r, t};
+                StepOut<float> o;
+                stepOnce(v, rhoScale, c, r, o, t, junk, n);
+                r = o.next;
+            }
+            after = r;
+        }
+        for (int step = last - 1; step >= first; --step) {
+            const Kept k = ring[step - first];
+            StepOut<float> o;
+            o.next = after;
+            o.k1 = bendAt(c, k.s.u);
+            accelOf(a, c.big, k.s.n, o.a1);
+            StepBar b;
+            memset(&b, 0, sizeof b);
+            b.nextU = next.u;
+            for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
+            b.nextPsi = next.psi;
+            b.nextDrag = next.drag;
+            if (escaped && step == steps - 1 && f.stars > 0.f)
+                skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
+            Crossing<float> x;
+            if (crossingOf(f, rhoScale, c, k.s, o, x))
+                crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
+            radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w, b.psi,
+                       b.drag, g);
+            polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
+            next = b;
+            after = k.s;
+        }
+    }
+    float grad[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    startBack(v, nx, ny, c, next, g, grad);
+    for (int q = 0; q < 5; ++q) acc[1 + q] += grad[q];
+    if (v.pixelGrads)
+        for (int q = 0; q < 5; ++q) v.pixelGrads[(size_t)i * 5 + q] = grad[q];
+    tally.rays += 1;
+    tally.steps += (unsigned)steps;
+    tally.crossings += crossings;
+    tally.escapes += escaped;
+}
+
+/* A warp an 8 x 4 tile of pixels (rays of neighbouring pixels take similar numbers of steps, so a warp's
+ * lanes stay busy together), a block four tiles of one view (blockIdx.y).  Each warp writes its tile's
+ * sums to the tile's own slot and leaves: no warp waits for another once the view is in shared memory.
+ * (A persistent grid taking tiles from a device counter measured slower: its warps hold more ray state
+ * resident at once.) */
 __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L) {
     __shared__ AdjointView v;
     {
@@ -705,130 +814,30 @@ __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L)
         for (int k = threadIdx.x; k < (int)(sizeof(AdjointView) / 16); k += kThreads) dst[k] = src[k];
     }
     __syncthreads();
-    const Frame<float>& f = v.f;
-    const int i = (int)(blockIdx.x * kThreads + threadIdx.x);
+    const int lane = (int)(threadIdx.x & 31);
+    const int local = (int)(blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5));
+    if (local >= L.tilesPerView) return; /* the whole warp: its tile lies past the view */
+    const int px = (local % L.tilesX) * 8 + (lane & 7), py = (local / L.tilesX) * 4 + (lane >> 3);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     Tally tally;
-    if (i < v.pixels) {
-        const int px = i % f.width, py = i / f.width;
-        float nx, ny, moment;
-        samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
-        RayConst<float> c;
-        RayState<float> s;
-        rayStart(f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
-        const float a = f.a;
-        if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
-        const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
-        const int K = L.K;
-        Kept ring[kMaxK + 1];
-        Kept checkpoint[kMaxSegments];
-        /* forward: the segment's states, and each segment's first */
-        float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
-        int steps = 0;
-        unsigned crossings = 0;
-        bool escaped = false;
-        RayState<float> end = s;
-        for (int step = 0; step < kMaxSteps; ++step) {
-            if (step % K == 0) checkpoint[step / K] = Kept{s, through};
-            ring[step % K] = Kept{s, through};
-            StepOut<float> o;
-            stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
-            ++steps;
-            end = o.next;
-            if (0.f > o.next.u) {
-                const float part = s.u / (s.u - o.next.u);
-                float away[3], dir[3];
-                for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
-                skyDirection(away, s.psi + part * (o.next.psi - s.psi), dir);
-                if (f.stars > 0.f) shadeSky(f, v.map, c, dir, through, sum);
-                escaped = true;
-                break;
-            }
-            if (o.next.u > f.uHorizon || !(through > .004f)) break;
-            s = o.next;
-        }
-        const int lastFirst = ((steps - 1) / K) * K;
-        ring[steps - lastFirst] = Kept{end, through};
-        /* the loss, and its adjoint in the radiance */
-        const float4 want = v.target[i];
-        const float diff[3] = {sum[0] - want.x, sum[1] - want.y, sum[2] - want.z};
-        acc[0] = (diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]) * v.lossScale;
-        const float sumBar[3] = {2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale, 2.f * diff[2] * v.lossScale};
-        if (v.hdr) v.hdr[i] = make_float4(sum[0], sum[1], sum[2], 0.f);
-        const float throughEnd = through;
-        /* back, a segment at a time */
-        StepBar next;
-        memset(&next, 0, sizeof next);
-        ConstBar g;
-        memset(&g, 0, sizeof g);
-        float throughBar = 0.f;
-        for (int first = lastFirst; first >= 0; first -= K) {
-            const int last = min(first + K, steps); /* steps first .. last - 1 */
-            if (first != lastFirst) {
-                RayState<float> r = checkpoint[first / K].s;
-                float t = checkpoint[first / K].through, junk[3] = {0.f, 0.f, 0.f};
-                unsigned n = 0;
-                for (int step = first; step < last; ++step) {
-                    ring[step - first] = Kept{r, t};
-                    StepOut<float> o;
-                    stepOnce(v, rhoScale, c, r, o, t, junk, n);
-                    r = o.next;
-                }
-                ring[last - first] = Kept{r, t};
-            }
-            for (int step = last - 1; step >= first; --step) {
-                const Kept k = ring[step - first];
-                StepOut<float> o;
-                o.next = ring[step - first + 1].s;
-                o.k1 = bendAt(c, k.s.u);
-                accelOf(a, c.big, k.s.n, o.a1);
-                StepBar b;
-                memset(&b, 0, sizeof b);
-                b.nextU = next.u;
-                for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
-                b.nextPsi = next.psi;
-                b.nextDrag = next.drag;
-                if (escaped && step == steps - 1 && f.stars > 0.f)
-                    skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
-                Crossing<float> x;
-                if (crossingOf(f, rhoScale, c, k.s, o, x))
-                    crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
-                radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w, b.psi,
-                           b.drag, g);
-                polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
-                next = b;
-            }
-        }
-        startBack(v, nx, ny, c, next, g, acc + 1);
-        if (v.pixelGrads)
-            for (int q = 0; q < 5; ++q) v.pixelGrads[(size_t)i * 5 + q] = acc[1 + q];
-        tally.rays = 1, tally.steps = (unsigned)steps, tally.crossings = crossings, tally.escapes = escaped;
-    }
+    if (px < v.f.width && py < v.f.height) adjointRay(v, px, py, L.K, acc, tally);
     flushTally(tally, L.counters);
-    /* the block's sums, in a fixed order */
-    __shared__ float warpSums[kThreads / 32][6];
+    const size_t tile = (size_t)blockIdx.y * L.tilesPerView + local;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         float s = acc[k];
         for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
-        if ((threadIdx.x & 31) == 0) warpSums[threadIdx.x >> 5][k] = s;
-    }
-    __syncthreads();
-    if (threadIdx.x < 8) {
-        float s = 0.f;
-        if (threadIdx.x < 6)
-            for (int w = 0; w < kThreads / 32; ++w) s += warpSums[w][threadIdx.x];
-        L.partials[((size_t)blockIdx.y * L.blocksPerView + blockIdx.x) * 8 + threadIdx.x] = s;
+        if (lane == 0) L.partials[tile * 8 + k] = s;
     }
 }
 
-/* One block a view: its blocks' sums added in double, in a fixed order. */
-__global__ void __launch_bounds__(256) adjointSums(const float* partials, int blocksPerView, double* results) {
+/* One block a view: its tiles' sums added in double, in a fixed order. */
+__global__ void __launch_bounds__(256) adjointSums(const float* partials, int tilesPerView, double* results) {
     __shared__ double part[256];
-    const float* mine = partials + (size_t)blockIdx.x * blocksPerView * 8;
+    const float* mine = partials + (size_t)blockIdx.x * tilesPerView * 8;
     for (int k = 0; k < 6; ++k) {
         double s = 0.0;
-        for (int b = threadIdx.x; b < blocksPerView; b += 256) s += (double)mine[(size_t)b * 8 + k];
+        for (int b = threadIdx.x; b < tilesPerView; b += 256) s += (double)mine[(size_t)b * 8 + k];
         part[threadIdx.x] = s;
         __syncthreads();
         for (int width = 128; width > 0; width >>= 1) {
@@ -844,7 +853,7 @@ __global__ void __launch_bounds__(256) adjointSums(const float* partials, int bl
 
 size_t adjointViewBytes() { return sizeof(AdjointView); }
 
-int adjointBlocks(int pixels) { return (pixels + kThreads - 1) / kThreads; }
+int adjointTiles(int width, int height) { return ((width + 7) / 8) * ((height + 3) / 4); }
 
 void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* jacobian, double emissivity,
                      const float* map, const float* fluid, const float* target, float* hdr, float* pixelGrads) {
@@ -866,16 +875,19 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
     memcpy(slot, &v, sizeof v);
 }
 
-cudaError_t launchAdjoint(const void* table, int count, int pixels, int K, unsigned long long* counters,
+cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
                           float* partials, double* results, cudaStream_t stream) {
     AdjointLaunch L;
     L.views = (const AdjointView*)table;
     L.partials = partials;
     L.counters = counters;
-    L.blocksPerView = adjointBlocks(pixels);
+    L.tilesX = (width + 7) / 8;
+    L.tilesPerView = adjointTiles(width, height);
+    L.totalTiles = L.tilesPerView * count;
     L.K = K;
-    adjointPixels<<<dim3((unsigned)L.blocksPerView, (unsigned)count), kThreads, 0, stream>>>(L);
-    adjointSums<<<count, 256, 0, stream>>>(partials, L.blocksPerView, results);
+    const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
+    adjointPixels<<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
+    adjointSums<<<count, 256, 0, stream>>>(partials, L.tilesPerView, results);
     return cudaGetLastError();
 }
 

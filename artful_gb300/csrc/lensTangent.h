@@ -27,12 +27,12 @@ cudaError_t launchTangents(const TraceLaunch& l, const double* jacobian, double 
 
 /* The adjoint's view table: one entry of adjointViewBytes() a view, filled on the host. */
 size_t adjointViewBytes();
-int adjointBlocks(int pixels);
+int adjointTiles(int width, int height); /* 8 x 4 tiles of pixels a view */
 void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* jacobian, double emissivity,
                      const float* map, const float* fluid, const float* target, float* hdr, float* pixelGrads);
-/* The adjoint over `count` views of `pixels` pixels each; partials: count * adjointBlocks(pixels) * 8
+/* The adjoint over `count` views of width x height; partials: count * adjointTiles(width, height) * 8
  * floats of scratch; results: count * 8 doubles (the loss, the five gradient components, two unused). */
-cudaError_t launchAdjoint(const void* table, int count, int pixels, int K, unsigned long long* counters,
+cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
                           float* partials, double* results, cudaStream_t stream);
 
 }  // namespace artf
