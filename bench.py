@@ -8,7 +8,12 @@ step, outside the timed region.  `e2e` is the same metric through the host-buffe
 (artfCudaHoleRender): the map and fluid copied from pinned host memory and the HDR frame copied back,
 every step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Beside it, on rank 0: the 64-view batch (one graph-captured persistent launch, autotuned); the adjoint at
+512 x 288 (its time over the forward trace's); and 32 inverse fits of 256 x 144 by Adam on the adjoint's
+gradients, with their recovery error and wall time per fit beside the same fit on FP64 central
+differences.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--fd-fits F]
 
 --impl reference times the reference's CPU path on this host's cores: the oracle port (the reference's
 own sources are not on this machine), with all host threads, on a bounded sample of the same frame.
@@ -47,6 +52,8 @@ def parse():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--sweep", action="store_true",
                    help="time the mixed trace's guard, band and batch variants, each with its endpoint error")
+    p.add_argument("--fd-fits", type=int, default=4,
+                   help="fits of the inverse-fit workload also run with FP64 central-difference gradients")
     return p.parse_args()
 
 
@@ -393,9 +400,12 @@ def main():
 
     cpu = None
     batch = None
+    adjoint = fitting = None
     if rank == 0 and not args.quick:
         cpu = cpu_baseline(scene, frame, map_, fluid, rays)
         batch = batch_measurement(lib, ctx, args.steps, flush)
+        adjoint = adjoint_measurement(lib, ctx, args.steps, flush)
+        fitting = fit_measurement(lib, ctx, args.fd_fits)
 
     lib.artfCudaDestroy(ctx)
     if rank != 0:
@@ -428,7 +438,116 @@ def main():
         line["cpu_baseline"] = cpu
     if batch:
         line["batch_64_views"] = batch
+    if adjoint:
+        line["adjoint"] = adjoint
+    if fitting:
+        line["inverse_fit"] = fitting
     print(json.dumps(line), flush=True)
+
+
+def _median_ms(run, steps, flush=None):
+    """Median over `steps` runs of the device time a run reports (its own CUDA events), after a flush of L2
+    before each when a flush buffer is given."""
+    times = []
+    for _ in range(max(3, steps)):
+        if flush is not None:
+            flush.fill_(1)
+        times.append(run())
+    return statistics.median(times)
+
+
+def adjoint_measurement(lib, ctx, steps, flush):
+    """Configuration 4: the adjoint at 512 x 288 (a = 0.6, i = 55 deg, r_in = 1.1 r_ISCO, q = 2.7,
+    r_obs = 32 against the image of a = 0.7, i = 60 deg, r_in = r_ISCO, q = 3, r_obs = 30), checkpoints
+    every 32 steps, beside the forward traces of the same rays (FP32 and mixed precision); and eight such
+    views in one adjoint launch beside one forward trace of as many pixels."""
+    import torch
+    from artful_gb300 import capi, fit
+    target, start = fit.config4_params()
+    m = fit.param_map(start)
+    capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
+    w, h = 512, 288
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    targets = adj.render([target])
+    torch.cuda.synchronize()
+    last = {}
+
+    def run_adjoint(views, tg):
+        def go():
+            loss, grad, st = adj(views, tg)
+            last.update(loss=loss, grad=grad, stats=st)
+            return st.ms
+        return go
+
+    def run_forward(p, width, height, precision):
+        f, f64, _ = fit.frames(p, width, height)
+        hdr = torch.empty((height, width, 4), dtype=torch.float32, device="cuda")
+        opts = capi.TraceOptions(precision, 0, 0, 1.0, 0.0, 0, 0, 0, 0, 0, 0)
+
+        def go():
+            s = capi.TraceStats()
+            capi.check(lib.artfCudaHoleTrace(ctx, C.byref(f), C.byref(f64), None, None, C.byref(opts), hdr.data_ptr(),
+                                             None, C.byref(s)))
+            last["fwd_steps"] = s.steps
+            return s.ms
+        return go
+
+    ms_adj = _median_ms(run_adjoint([start], targets), steps, flush)
+    one = dict(last)
+    ms_fp32 = _median_ms(run_forward(start, w, h, capi.FP32), steps, flush)
+    ms_mixed = _median_ms(run_forward(start, w, h, capi.MIXED), steps, flush)
+    eight = targets.repeat(8, 1, 1, 1)
+    ms_adj8 = _median_ms(run_adjoint([start] * 8, eight), steps, flush)
+    steps8 = last["stats"].steps
+    ms_fp32_big = _median_ms(run_forward(start, 1448, 816, capi.FP32), steps, flush)
+    return {
+        "workload": "512x288, 1 ray at each pixel centre, loss = MSE of linear RGB against the target's image, K=32",
+        "adjoint_ms": ms_adj, "forward_fp32_ms": ms_fp32, "forward_mixed_ms": ms_mixed,
+        "adjoint_over_forward_fp32": ms_adj / ms_fp32, "adjoint_over_forward_mixed": ms_adj / ms_mixed,
+        "steps": one["stats"].steps, "loss": float(one["loss"][0]),
+        "gradient": dict(zip(fit.PARAM_NAMES, map(float, one["grad"][0]))),
+        "batched_8_views": {"adjoint_ms": ms_adj8, "steps": steps8,
+                            "forward_fp32_1448x816_ms": ms_fp32_big,
+                            "adjoint_over_forward_fp32": ms_adj8 / ms_fp32_big},
+    }
+
+
+def fit_measurement(lib, ctx, fd_fits):
+    """Configuration 5: 32 independent fits of 256 x 144 (targets from seed 3, starts 15% off in every
+    parameter), 200 Adam steps of lr 1e-2, every step one adjoint launch over all 32 views; beside the same
+    fit with gradients by central differences (h = 1e-4) of FP64 renders, on the first `fd_fits` fits."""
+    import torch
+    from artful_gb300 import capi, fit
+    fits = fit.config5_fits(32, seed=3)
+    m = fit.param_map(fits[0][0])
+    capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
+    w, h = 256, 144
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    fit.fit_batch(adj, fits[:2], steps=3)  # warm-up
+    theta, history, wall = fit.fit_batch(adj, fits, steps=200, lr=1e-2)
+    err = fit.recovery_error(theta, fits)
+
+    def summary(e):
+        return {"median": dict(zip(fit.PARAM_NAMES, map(float, np.median(e, 0)))),
+                "p90": dict(zip(fit.PARAM_NAMES, map(float, np.percentile(e, 90, 0)))),
+                "fits_within_5pct": int((e.max(1) < 0.05).sum()), "fits_within_10pct": int((e.max(1) < 0.10).sum())}
+
+    out = {"workload": "32 fits of 256x144, 200 Adam steps, lr 1e-2 (relative to the start), adjoint K=32",
+           "wall_s": wall, "wall_per_fit_s": wall / len(fits), "start_error": 0.15,
+           "loss_first_last": [float(history[0]), float(history[-1])], "recovery_error": summary(err)}
+    if fd_fits > 0:
+        targets = adj.render([t for t, _ in fits[:fd_fits]])
+        fp64 = fit.Fp64Loss(lib, ctx, w, h, m, lib.artfCudaDeviceFluid(ctx), 11 * fd_fits)
+        theta_fd, history_fd, wall_fd = fit.fit_batch_fd(fp64, fits[:fd_fits], targets, steps=200, lr=1e-2)
+        err_fd = fit.recovery_error(theta_fd, fits[:fd_fits])
+        out["fp64_fd_baseline"] = {
+            "fits": fd_fits, "wall_s": wall_fd, "wall_per_fit_s": wall_fd / fd_fits,
+            "loss_first_last": [float(history_fd[0]), float(history_fd[-1])],
+            "recovery_error": summary(err_fd), "adjoint_same_fits": summary(err[:fd_fits]),
+            "adjoint_speedup_per_fit": (wall_fd / fd_fits) / (wall / len(fits))}
+        del fp64
+        torch.cuda.empty_cache()
+    return out
 
 
 def batch_measurement(lib, ctx, steps, flush):
