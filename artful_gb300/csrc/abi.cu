@@ -55,6 +55,9 @@ struct ArtfCuda {
     bool stagedPending;
     ArtfCudaTuning tuned;
     bool hasTuning;
+    /* the mixed trace's ray planes (one float4 a ray of a pixel), for views of several rays a pixel */
+    float4* planes;
+    size_t planeCount;
     /* the adjoint's view table (device and pinned staging), block sums and per-view results */
     void* adjTable;
     void* adjStage;
@@ -140,6 +143,7 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->bloom);
     cudaFree(ctx->table);
     cudaFreeHost(ctx->stage);
+    cudaFree(ctx->planes);
     cudaFree(ctx->adjTable);
     cudaFreeHost(ctx->adjStage);
     cudaFree(ctx->adjPartials);
@@ -256,22 +260,51 @@ static int reserveTable(ArtfCuda* ctx, int count) {
     return ARTF_CUDA_OK;
 }
 
-/* Fills the staging table from views; the total queue units in *units. */
+/* The ray planes a batch of views needs (float4 each). */
+static size_t planesOf(const artf::TraceLaunch& l, const ArtfCudaView* views, int count) {
+    size_t total = 0;
+    for (int i = 0; i < count; ++i)
+        total += (size_t)views[i].frame.size[0] * views[i].frame.size[1] * artf::mixedRayPlanes(l, views[i].frame);
+    return total;
+}
+
+/* Room for `count` float4 of ray planes in the context. */
+static int reservePlanes(ArtfCuda* ctx, size_t count) {
+    if (count <= ctx->planeCount) return ARTF_CUDA_OK;
+    cudaFree(ctx->planes); /* (synchronises: no launch still writes the old planes) */
+    ctx->planes = nullptr;
+    ctx->planeCount = 0;
+    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->planes, sizeof(float4) * count));
+    ctx->planeCount = count;
+    return ARTF_CUDA_OK;
+}
+
+/* Fills the staging table from views; the total queue units in *units.  planes: room for the views' ray
+ * planes (planesOf), or NULL to trace a pixel a unit; *combinePixels: the largest view with planes. */
 static int fillTable(ArtfCuda* ctx, const artf::TraceLaunch& l, const ArtfCudaView* views, int count,
-                     const ArtfCudaTraceOptions* o, void* stage, int* units) {
+                     const ArtfCudaTraceOptions* o, void* stage, float4* planes, int* units, size_t* combinePixels) {
     long long total = 0;
+    size_t offset = 0, widest = 0;
     for (int i = 0; i < count; ++i) {
         const ArtfCudaView& v = views[i];
         if (int s = checkFrame(&v.frame, o)) return s;
         if (!v.hdr) return fail(ARTF_CUDA_EINVAL, "view %d: hdr is NULL", i);
         if ((!v.map && !ctx->mapHeld) || (!v.fluid && !ctx->fluidHeld))
             return fail(ARTF_CUDA_EINVAL, "view %d: no map or fluid, and none set on the context", i);
+        const size_t pixels = (size_t)v.frame.size[0] * v.frame.size[1], np = artf::mixedRayPlanes(l, v.frame);
+        float4* rayOut = planes && np ? planes + offset : nullptr;
+        if (rayOut) {
+            offset += pixels * np;
+            widest = pixels > widest ? pixels : widest;
+        }
         const int n = artf::mixedFillView(l, v.frame, v.frame64, v.map ? v.map : ctx->map, v.fluid ? v.fluid : ctx->fluid,
-                                          (float4*)v.hdr, v.ends, (int)total, (char*)stage + artf::mixedViewBytes() * i);
+                                          (float4*)v.hdr, v.ends, rayOut, (int)total,
+                                          (char*)stage + artf::mixedViewBytes() * i);
         total += n;
-        if (total > 0x7FFFFFFFLL) return fail(ARTF_CUDA_EINVAL, "batch of %lld pixels is too large", total);
+        if (total > 0x7FFFFFFFLL) return fail(ARTF_CUDA_EINVAL, "batch of %lld rays is too large", total);
     }
     *units = (int)total;
+    *combinePixels = widest;
     return ARTF_CUDA_OK;
 }
 
@@ -316,12 +349,17 @@ static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCuda
     if (int s = spendLaunch(ctx)) return s;
     if (precision == ARTF_CUDA_MIXED) {
         if (int s = reserveTable(ctx, 1)) return s;
+        const size_t pixels = (size_t)l.frame.size[0] * l.frame.size[1];
+        const size_t np = l.rayCount > 0 ? 0 : artf::mixedRayPlanes(l, l.frame);
+        if (np)
+            if (int s = reservePlanes(ctx, pixels * np)) return s;
         if (int s = waitStaging(ctx)) return s;
-        const int units = artf::mixedFillView(l, l.frame, l.frame64, l.map, l.fluid, l.hdr, l.ends, 0, ctx->stage);
+        const int units = artf::mixedFillView(l, l.frame, l.frame64, l.map, l.fluid, l.hdr, l.ends,
+                                              np ? ctx->planes : nullptr, 0, ctx->stage);
         if (int s = sendTable(ctx, 1)) return s;
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "mixed trace launch: %s", cudaGetErrorString(e));
     } else {
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
@@ -602,13 +640,15 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     if ((status = spendLaunch(ctx))) return status;
     const artf::TraceLaunch l = launchOf(ctx, options);
     if ((status = reserveTable(ctx, count))) return status;
+    if ((status = reservePlanes(ctx, planesOf(l, views, count)))) return status;
     if ((status = waitStaging(ctx))) return status;
     int units = 0;
-    if ((status = fillTable(ctx, l, views, count, options, ctx->stage, &units))) return status;
+    size_t combine = 0;
+    if ((status = fillTable(ctx, l, views, count, options, ctx->stage, ctx->planes, &units, &combine))) return status;
     if ((status = sendTable(ctx, count))) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units);
+    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
@@ -617,10 +657,13 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
 struct ArtfCudaGraph {
     ArtfCuda* ctx;
     int count, units;
+    size_t combine;
     ArtfCudaTraceOptions options;
     ArtfCudaHoleFrame first; /* (for the stats' counting rule) */
     void* table;
     void* stage;
+    float4* planes; /* the graph's own ray planes: its captured launches keep the pointer */
+    size_t planeCount;
     cudaGraph_t graph;
     cudaGraphExec_t exec;
 };
@@ -633,6 +676,7 @@ extern "C" void artfCudaBatchGraphDestroy(ArtfCudaGraph* g) {
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->table);
     cudaFreeHost(g->stage);
+    cudaFree(g->planes);
     free(g);
 }
 
@@ -651,11 +695,14 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
     g->first = views[0].frame;
     const size_t bytes = artf::mixedViewBytes() * (size_t)count;
     const artf::TraceLaunch l = launchOf(ctx, options);
-    if (cudaMalloc(&g->table, bytes) != cudaSuccess || cudaMallocHost(&g->stage, bytes) != cudaSuccess) {
+    const size_t planes = planesOf(l, views, count);
+    g->planeCount = planes;
+    if (cudaMalloc(&g->table, bytes) != cudaSuccess || cudaMallocHost(&g->stage, bytes) != cudaSuccess ||
+        (planes && cudaMalloc(&g->planes, sizeof(float4) * planes) != cudaSuccess)) {
         artfCudaBatchGraphDestroy(g);
         return fail(ARTF_CUDA_ENOMEM, "graph table allocation");
     }
-    if ((status = fillTable(ctx, l, views, count, options, g->stage, &g->units))) {
+    if ((status = fillTable(ctx, l, views, count, options, g->stage, g->planes, &g->units, &g->combine))) {
         artfCudaBatchGraphDestroy(g);
         return status;
     }
@@ -663,7 +710,7 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
     if (e == cudaSuccess) {
         cudaMemcpyAsync(g->table, g->stage, bytes, cudaMemcpyHostToDevice, ctx->stream);
         cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
-        artf::launchMixedTable(l, g->table, count, g->units);
+        artf::launchMixedTable(l, g->table, count, g->units, g->combine);
         e = cudaStreamEndCapture(ctx->stream, &g->graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
@@ -685,8 +732,13 @@ extern "C" int artfCudaBatchGraphUpdate(ArtfCudaGraph* g, const ArtfCudaView* vi
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(g->ctx->stream));
     const artf::TraceLaunch l = launchOf(g->ctx, &g->options);
     int units = 0;
-    if ((status = fillTable(g->ctx, l, views, count, &g->options, g->stage, &units))) return status;
-    if (units != g->units) return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
+    size_t combine = 0;
+    /* (the planes the graph holds must cover the new views: sizes may differ at equal tile counts) */
+    if (planesOf(l, views, count) != g->planeCount)
+        return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
+    if ((status = fillTable(g->ctx, l, views, count, &g->options, g->stage, g->planes, &units, &combine))) return status;
+    if (units != g->units || combine != g->combine)
+        return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
     g->first = views[0].frame;
     return ARTF_CUDA_OK;
 }
@@ -706,13 +758,14 @@ extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* st
 /* ---- the autotuner ------------------------------------------------------------------------------ */
 
 /* Median time of `repeats` launches of the batch already in the context's table. */
-static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int units, int repeats, float* ms) {
+static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int units, size_t combine, int repeats,
+                     float* ms) {
     float times[8];
     for (int r = -1; r < repeats; ++r) {
         CUDA_OR(ARTF_CUDA_ELAUNCH,
                 cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "autotune launch: %s", cudaGetErrorString(e));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->stop));
@@ -739,9 +792,11 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
     ctx->hasTuning = false;
     artf::TraceLaunch l = launchOf(ctx, &o);
     if ((status = reserveTable(ctx, count))) return status;
+    if ((status = reservePlanes(ctx, planesOf(l, views, count)))) return status;
     if ((status = waitStaging(ctx))) return status;
     int units = 0;
-    if ((status = fillTable(ctx, l, views, count, &o, ctx->stage, &units))) return status;
+    size_t combine = 0;
+    if ((status = fillTable(ctx, l, views, count, &o, ctx->stage, ctx->planes, &units, &combine))) return status;
     if ((status = sendTable(ctx, count))) return status;
 
     /* coordinate descent over the launch shape, from the defaults */
@@ -756,7 +811,7 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
     float bestMs = 0.f;
     int trials = 0;
     l.blockSize = best[0], l.compactEvery = best[1], l.fp64Batch = best[2], l.refillBatch = best[3];
-    if ((status = timeBatch(ctx, l, count, units, repeats, &bestMs))) return status;
+    if ((status = timeBatch(ctx, l, count, units, combine, repeats, &bestMs))) return status;
     const float defaultMs = bestMs;
     ++trials;
     for (int pass = 0; pass < 2; ++pass)
@@ -767,7 +822,7 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
                 trial[d] = values[d][c];
                 l.blockSize = trial[0], l.compactEvery = trial[1], l.fp64Batch = trial[2], l.refillBatch = trial[3];
                 float ms = 0.f;
-                if ((status = timeBatch(ctx, l, count, units, repeats, &ms))) return status;
+                if ((status = timeBatch(ctx, l, count, units, combine, repeats, &ms))) return status;
                 ++trials;
                 if (ms < bestMs * 0.99f) {
                     bestMs = ms;

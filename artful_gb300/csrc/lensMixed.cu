@@ -42,8 +42,12 @@ struct MixedView {
     const float* fluid;
     float4* hdr;
     ArtfCudaRayEnd* ends;
+    /* Rays of the view's pixels, plane k for ray k (radiance, class bits), or NULL.  With planes, a work
+     * unit is one ray and mixedCombine sums each pixel's rays afterwards; without, a unit is a pixel
+     * whose rays one lane traces in turn. */
+    float4* rayOut;
     float rhoScale, uGuard, share;
-    int tilesX, units, unitBase, rays, jitter;
+    int tilesX, pixelUnits, units, unitBase, rays, jitter;
     uint32_t seed;
 };
 static_assert(sizeof(MixedView) <= kMixedViewBytesMax, "a view table slot outgrew kMixedViewBytesMax");
@@ -276,7 +280,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     const unsigned below = (1u << lane) - 1u;
     Tally t;
     Reasons n;
-    int unit = -1, x = 0, y = 0, k = 0, rays = 1;
+    int unit = -1, x = 0, y = 0, k = 0, kEnd = 1; /* this lane's unit: rays k .. kEnd - 1 of pixel (x, y) */
     const MixedView* v = p.views;
     bool exhausted = false, live = false, haveStep = false, waitR = false, waitP = false;
     unsigned reason = 0, bits = 0;
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         const unsigned liveMask = __ballot_sync(full, live);
         if (idle && (__popc(idle) >= p.refill || liveMask == 0 || sinceStart >= p.maxWait)) {
             sinceStart = 0;
-            const bool needPixel = !live && !exhausted && (unit < 0 || k >= rays);
+            const bool needPixel = !live && !exhausted && (unit < 0 || k >= kEnd);
             const unsigned fetch = __ballot_sync(full, needPixel);
             if (fetch) {
                 const int leader = __ffs(fetch) - 1;
@@ -308,15 +312,20 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                         unit = -1;
                     } else {
                         v = p.views + viewOf(p, unit);
-                        const int local = unit - v->unitBase, tile = local >> 5, within = local & 31;
+                        int local = unit - v->unitBase;
+                        /* with ray planes the units run ray-major: a warp's lanes take neighbouring pixels */
+                        const int plane = v->rayOut ? local / v->pixelUnits : 0;
+                        local -= plane * v->pixelUnits;
+                        const int tile = local >> 5, within = local & 31;
                         x = (tile % v->tilesX) * 8 + (within & 7);
                         y = (tile / v->tilesX) * 4 + (within >> 3);
-                        rays = v->rays;
-                        if (x >= v->f.width || y >= v->f.height) k = rays; /* (off the image: fetch again) */
+                        k = plane;
+                        kEnd = v->rayOut ? plane + 1 : v->rays;
+                        if (x >= v->f.width || y >= v->f.height) k = kEnd; /* (off the image: fetch again) */
                     }
                 }
             }
-            if (!live && unit >= 0 && k < rays) {
+            if (!live && unit >= 0 && k < kEnd) {
                 float nx, ny, moment;
                 samplePosition(v->h, v->jitter, v->seed, x, y, k, &nx, &ny, &moment);
                 mixedStart(p, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
@@ -366,18 +375,43 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
             const unsigned ended = mixedAdvance(p, *v, r, o);
             if (ended) {
                 const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
-                ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)rays + (size_t)k : nullptr;
-                bits |= classBits(mixedFinish(r, ended, end, t));
-                for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
+                ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)v->rays + (size_t)k : nullptr;
+                const unsigned rayBits = classBits(mixedFinish(r, ended, end, t));
                 live = false;
-                if (++k == rays)
-                    v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share, pixel[2] * v->share,
-                                                (float)bits);
+                if (v->rayOut) {
+                    const size_t plane = (size_t)v->f.width * (size_t)v->f.height;
+                    v->rayOut[(size_t)k * plane + index] = make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
+                    ++k;
+                } else {
+                    bits |= rayBits;
+                    for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
+                    if (++k == kEnd)
+                        v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share, pixel[2] * v->share,
+                                                    (float)bits);
+                }
             }
         }
     }
     flushTally(t, p.counters);
     flushReasons(n, p.counters);
+}
+
+/* Each pixel of the views with ray planes: its rays' radiance summed in ray order and scaled by
+ * 1 / rays, and their class bits; the same operations, in the same order, as the per-pixel path. */
+__global__ void __launch_bounds__(256) mixedCombine(const MixedView* views) {
+    const MixedView& v = views[blockIdx.y];
+    if (!v.rayOut) return;
+    const size_t pixels = (size_t)v.f.width * (size_t)v.f.height;
+    const size_t i = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= pixels) return;
+    float sum[3] = {0.f, 0.f, 0.f};
+    unsigned bits = 0;
+    for (int k = 0; k < v.rays; ++k) {
+        const float4 q = v.rayOut[(size_t)k * pixels + i];
+        sum[0] = sum[0] + q.x, sum[1] = sum[1] + q.y, sum[2] = sum[2] + q.z;
+        bits |= (unsigned)q.w;
+    }
+    v.hdr[i] = make_float4(sum[0] * v.share, sum[1] * v.share, sum[2] * v.share, (float)bits);
 }
 
 /* The per-ray entry point: rays at given image positions in the table's first view. */
@@ -416,7 +450,8 @@ MixedParams paramsOf(const TraceLaunch& l, const void* deviceTable, int viewCoun
 size_t mixedViewBytes() { return sizeof(MixedView); }
 
 int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
-                  const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, int unitBase, void* slot) {
+                  const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, float4* rayOut, int unitBase,
+                  void* slot) {
     MixedView v;
     memset(&v, 0, sizeof v);
     v.f.load(frame64, frame);
@@ -433,7 +468,9 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.jitter = l.jitter;
     v.seed = l.seed;
     v.tilesX = ((int)frame.size[0] + 7) / 8;
-    v.units = v.tilesX * (((int)frame.size[1] + 3) / 4) * 32;
+    v.pixelUnits = v.tilesX * (((int)frame.size[1] + 3) / 4) * 32;
+    v.rayOut = v.rays > 1 ? rayOut : nullptr; /* (one ray a pixel: the pixel is the ray) */
+    v.units = v.pixelUnits * (v.rayOut ? v.rays : 1);
     v.unitBase = unitBase;
     memcpy(slot, &v, sizeof v);
     return v.units;
@@ -448,7 +485,8 @@ int mixedGrid(const TraceLaunch& l, int totalUnits) {
     return grid > needed ? needed : (grid < 1 ? 1 : grid);
 }
 
-cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits) {
+cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits,
+                             size_t combinePixels) {
     const MixedParams p = paramsOf(l, deviceTable, viewCount, totalUnits);
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
@@ -457,6 +495,8 @@ cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int 
         return cudaGetLastError();
     }
     traceMixedQueue<<<mixedGrid(l, totalUnits), block, 0, l.stream>>>(p);
+    if (combinePixels > 0)
+        mixedCombine<<<dim3((unsigned)((combinePixels + 255) / 256), (unsigned)viewCount), 256, 0, l.stream>>>(p.views);
     return cudaGetLastError();
 }
 

@@ -14,16 +14,26 @@
 namespace artf {
 
 /* A table slot never takes more than this (lensMixed.cu checks it at compile time). */
-constexpr size_t kMixedViewBytesMax = 1024;
+constexpr size_t kMixedViewBytesMax = 1152;
 
 size_t mixedViewBytes();
-/* Fills one table slot; returns the view's unit count. */
+/* Fills one table slot; returns the view's unit count.  rayOut: the view's ray planes (width * height
+ * float4 a ray of a pixel, mixedRayPlanes of them), or NULL.  With planes a work unit is one ray, so
+ * no lane is left with a pixel's several long rays after the queue empties; without, a unit is a pixel. */
 int mixedFillView(const TraceLaunch& options, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
-                  const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, int unitBase, void* slot);
+                  const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, float4* rayOut, int unitBase,
+                  void* slot);
+/* The planes a view needs: rays a pixel when above one, else none. */
+inline size_t mixedRayPlanes(const TraceLaunch& l, const ArtfCudaHoleFrame& frame) {
+    const size_t rays = l.jitter ? (size_t)l.jitter : (size_t)frame.size[2] * frame.size[2];
+    return rays > 1 ? rays : 0;
+}
 /* The persistent grid for a batch of this many units. */
 int mixedGrid(const TraceLaunch& options, int totalUnits);
 /* Launches the trace of a table already on the device (or, with options.rayCount > 0, the ray list of
- * its first view). */
-cudaError_t launchMixedTable(const TraceLaunch& options, const void* deviceTable, int viewCount, int totalUnits);
+ * its first view); then, when combinePixels (the largest view's pixel count) is above 0, the sum of
+ * the views' ray planes into their frames. */
+cudaError_t launchMixedTable(const TraceLaunch& options, const void* deviceTable, int viewCount, int totalUnits,
+                             size_t combinePixels);
 
 }  // namespace artf

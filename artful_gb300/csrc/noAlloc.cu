@@ -7,7 +7,7 @@
  * point keeps its only scratch, the batch's view table and its work-queue and tally counters, in one
  * file-scope device array of fixed size, and takes every input and output from the caller.
  *
- * The array lives on every GPU that loads the library until the process exits (66 KB).  Host code
+ * The array lives on every GPU that loads the library until the process exits (74 KB).  Host code
  * cannot use the array's name as a device address, so the first call on each device looks the address
  * up there (cudaGetSymbolAddress, with that device current) and keeps it: make that first call before
  * any stream capture.  All calls share the array and it keeps the last call's contents; each call
@@ -105,8 +105,9 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     alignas(16) unsigned char stage[ARTF_CUDA_NOALLOC_MAX_VIEWS * artf::kMixedViewBytesMax];
     long long units = 0;
     for (int i = 0; i < count; ++i) {
+        /* (no ray planes: the fixed scratch cannot hold them, so a work unit is a pixel) */
         units += artf::mixedFillView(l, views[i].frame, views[i].frame64, views[i].map, views[i].fluid,
-                                     (float4*)views[i].hdr, views[i].ends, (int)units,
+                                     (float4*)views[i].hdr, views[i].ends, nullptr, (int)units,
                                      stage + artf::mixedViewBytes() * (size_t)i);
         if (units > 0x7FFFFFFFLL) return artf::failWith(ARTF_CUDA_EINVAL, "batch is too large");
     }
@@ -114,7 +115,7 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     cudaError_t e = cudaMemcpyAsync(table, stage, artf::mixedViewBytes() * (size_t)count, cudaMemcpyHostToDevice,
                                     l.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kCounterBytes, l.stream);
-    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units);
+    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0);
     if (e != cudaSuccess) {
         snprintf(line, sizeof line, "allocation-free batch launch: %s", cudaGetErrorString(e));
         return artf::failWith(ARTF_CUDA_ELAUNCH, line);

@@ -46,10 +46,12 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--quick", action="store_true", help="skip the slow side measurements")
-    p.add_argument("--profile", choices=["mixed", "fp64", "exact", "fp32"],
-                   help="trace one frame of that precision (after one untimed one) and exit: the case for ncu")
+    p.add_argument("--profile", choices=["mixed", "fp64", "exact", "fp32", "adjoint"],
+                   help="trace one frame of that precision (after one untimed one), or run the adjoint twice, "
+                        "and exit: the case for ncu")
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--views", type=int, default=1, help="views of --profile adjoint")
     p.add_argument("--sweep", action="store_true",
                    help="time the mixed trace's guard, band and batch variants, each with its endpoint error")
     p.add_argument("--fd-fits", type=int, default=4,
@@ -130,12 +132,28 @@ def sweep(args):
 
 
 def profile_case(args):
-    """One warm-up and one traced frame of one precision at the given size, nothing else."""
+    """One warm-up and one traced frame of one precision at the given size, nothing else; or, for
+    `adjoint`, two adjoint launches over `--views` views of the adjoint workload at the given size."""
     from artful_gb300 import capi, scenes
     import torch
     lib = capi.load()
     ctx = C.c_void_p()
     capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
+    if args.profile == "adjoint":
+        from artful_gb300 import fit
+        target, start = fit.config4_params()
+        m = fit.param_map(start)
+        capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 1))
+        unit = scenes.unit_fluid()
+        capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 1))
+        adj = fit.Adjoint(lib, ctx, args.width, args.height, checkpoint=32)
+        targets = adj.render([target] * args.views)
+        for _ in range(2):
+            loss, grad, s = adj([start] * args.views, targets)
+        print(json.dumps({"profile": "adjoint", "width": args.width, "height": args.height, "views": args.views,
+                          "ms": s.ms, "rays": s.rays, "steps": s.steps, "grad": grad[0].tolist()}))
+        lib.artfCudaDestroy(ctx)
+        return
     scene = scenes.config2(4)
     scene.width, scene.height = args.width, args.height
     frame, frame64, clamped = scenes.frame(scene)

@@ -301,7 +301,7 @@ void artfCudaBatchGraphDestroy(ArtfCudaGraph* graph);
  * the current device and on the caller's `stream` (a cudaStream_t, or NULL), and every view's map,
  * fluid and hdr must be device pointers the caller owns.  Its scratch (the view table and the queue
  * counters) is one fixed array on each device that loads the library, held until the process exits
- * (66 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
+ * (74 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
  * ARTF_CUDA_EINVAL.  The first call on each device looks up the array's device address there; make it
  * before any stream capture.  Calls share the array: calls whose work overlaps on the GPU race, so order
  * them on one stream.  Asynchronous; stats, when given, synchronises the stream and fills the counts
