@@ -1,27 +1,33 @@
 /* artful_cuda — the algorithmic work of a trace, for the roofline.
  *
- * Counting rule: each float + - * / sqrt min max is one operation (a fused multiply-add two);
- * comparisons, floor, abs, conversions, integer work and loads are not counted; loop-invariant
- * products the compiler hoists are counted once per ray.  The constants are an exact count of the
- * formulas in lensCore.cuh (tests/test_flops.py evaluates those formulas on the host with an
- * operation-counting number type and checks every constant here).
+ * Counting rule: each float + - * / sqrt min max is one operation (a fused multiply-add two; a
+ * reciprocal square root a square root and a division); comparisons, floor, abs, sign flips,
+ * conversions, integer work and loads are not counted.  The constants are an exact count of the
+ * formulas in lensCore.cuh: tests/flops_count.cpp evaluates those formulas on the host with an
+ * operation-counting number type and tests/test_flops.py checks every constant here against it.
  *
- *   per ray      setup of the constants of motion and the first state (rayStart, the first drag, the
- *                disc's radial scale), and the pixel's sum
- *   per step     one Nystrom step with its frame-drag terms (spin != 0), and the plane test
- *   per crossing the crossing's position, three slices of the disc, the ring's heat and glow, the
- *                Doppler shift (doppler != 0) and the colour
- *   per escape   the escape direction, and the stars and sky dust (stars > 0) */
+ *   per ray      the set-up of the constants of motion and the first state (rayStart, the first drag,
+ *                the disc's radial scale); the 15 products of the ray's constants that each Nystrom
+ *                sub-step's formulas recompute (a^2, h^2, h/2, h^2/8, h^2/2, h^2/6, h/6 in both, 2a^2 in
+ *                the polar one), counted once a ray since they do not change along it; and the 3 sums
+ *                that add the ray's light to its pixel (the pixel's 3 products by 1 / rays not counted)
+ *   per step     one Nystrom step with its frame-drag terms (spin != 0), without those 15, and the
+ *                plane test n_z n_z'
+ *   per crossing an accepted crossing's position, three slices of the disc (all inside), the ring's
+ *                heat and glow, the Doppler shift (doppler != 0) and the colour
+ *   per escape   the escape point and the direction in the sky's frame; with stars > 0, the stars and
+ *                sky dust toward it where neither star layer draws a star there (a drawn star adds up to
+ *                63 more: counted as none, so the count is a lower bound there) */
 #pragma once
 
-#define ARTF_FLOPS_RAY 85
-#define ARTF_FLOPS_RAY_SPINLESS 74     /* spin 0: no initial drag */
+#define ARTF_FLOPS_RAY 100
+#define ARTF_FLOPS_RAY_SPINLESS 88     /* spin 0: no initial drag */
 #define ARTF_FLOPS_STEP 149
 #define ARTF_FLOPS_STEP_SPINLESS 122   /* spin 0: no drag, no psi */
-#define ARTF_FLOPS_CROSSING 395
+#define ARTF_FLOPS_CROSSING 375
 #define ARTF_FLOPS_CROSSING_DOPPLER 26 /* of those, the Doppler shift's */
-#define ARTF_FLOPS_ESCAPE 63
-#define ARTF_FLOPS_SKY 61
+#define ARTF_FLOPS_ESCAPE 59
+#define ARTF_FLOPS_SKY 58
 
 static inline double artfFlops(unsigned long long rays, unsigned long long steps, unsigned long long crossings,
                                unsigned long long escapes, int spinning, int doppler, int stars) {
