@@ -35,6 +35,7 @@ UNITS = {
     "post.cu": EXACT,
     "lensTangent.cu": [],
     "lensAdjoint.cu": FAST,
+    "fluid.cu": EXACT,
 }
 C_UNITS = ["holeHost.c", "renderer.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]

@@ -161,6 +161,13 @@ SIGNATURES = {
     "artfCudaHoleTangents": (C.c_int, [_vp, P(HoleParams), P(HoleFrame), P(HoleFrame64), _vp, _vp, _vp, _vp]),
     "artfCudaHoleAdjoint": (C.c_int, [_vp, P(HoleParams), C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp,
                                       _vp, P(AdjointResult), P(TraceStats)]),
+    # the disc's fluid on the GPU
+    "artfCudaFluidNew": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_double, P(_vp)]),
+    "artfCudaFluidAdvance": (C.c_int, [_vp, C.c_double, P(C.c_int)]),
+    "artfCudaFluidField": (_vp, [_vp]),
+    "artfCudaFluidTime": (C.c_double, [_vp]),
+    "artfCudaFluidRead": (C.c_int, [_vp, _vp]),
+    "artfCudaFluidFree": (None, [_vp]),
     # the renderer backend (artful_cuda_renderer.h)
     "artfCudaNew": (_vp, [_vp]),
     "artfCudaNewWithReader": (_vp, [_vp, _vp]),

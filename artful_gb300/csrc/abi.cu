@@ -616,6 +616,12 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
 /* For the other C ABI units (noAlloc.cu): the same error line and argument checks. */
 namespace artf {
 int failWith(int status, const char* message) { return fail(status, "%s", message); }
+/* For the other units that work on a context (fluid.cu): its device made current, and its stream. */
+int contextStream(ArtfCuda* ctx, cudaStream_t* stream) {
+    if (int s = enter(ctx)) return s;
+    *stream = ctx->stream;
+    return ARTF_CUDA_OK;
+}
 int checkTraceFrame(const ArtfCudaHoleFrame* frame, const ArtfCudaTraceOptions* options) {
     return checkFrame(frame, options);
 }

@@ -386,6 +386,27 @@ int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int cou
                         const float* map, const float* fluid, const float* targets, int checkpointEvery, float* hdr,
                         float* pixelGrads, ArtfCudaAdjointResult* results, ArtfCudaTraceStats* stats);
 
+/* ---- the disc's gas, stepped on the GPU (src/scene/fluid.c) --------------------------------------- */
+
+/* The reference steps the disc's fluid on the CPU every frame and uploads its 1 MB field; this one lives
+ * on the context's device, where the trace reads it, and its bytes equal the reference's (fluid.c is
+ * deterministic: + - * / and comparisons in a fixed order). */
+typedef struct ArtfCudaFluid ArtfCudaFluid;
+/* fluid.c:255 artfFluidNew: the gas of a disc from inner to outer around a hole of this spin, as of
+ * `time` (its start: 200 eddies and 60 steps).  Synchronous. */
+int artfCudaFluidNew(ArtfCuda* ctx, float inner, float outer, float spin, double time, ArtfCudaFluid** out);
+/* fluid.c:319 artfFluidAdvance: steps of 0.2 up to `time`, at most 48 a call (the gas does not run back);
+ * *stepped (may be NULL): whether the field changed.  On the context's stream. */
+int artfCudaFluidAdvance(ArtfCudaFluid* f, double time, int* stepped);
+/* fluid.c:335-336: the field (device, ARTF_CUDA_FLUID_FLOATS, owned by f; valid after the stream's work)
+ * and the moment it is of. */
+const float* artfCudaFluidField(const ArtfCudaFluid* f);
+double artfCudaFluidTime(const ArtfCudaFluid* f);
+/* The field copied to host memory.  Synchronous. */
+int artfCudaFluidRead(const ArtfCudaFluid* f, float* host);
+/* fluid.c:243 */
+void artfCudaFluidFree(ArtfCudaFluid* f);
+
 /* ---- measurement ------------------------------------------------------------------------------- */
 
 /* The device's FP32 and FP64 fused multiply-add throughput, measured (flop/s, a multiply-add two):

@@ -58,8 +58,38 @@ def oracle() -> C.CDLL:
         lib.oracleJitter.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.oraclePost.argtypes = [vp, vp, vp]
         lib.oracleThreads.restype = C.c_int
+        lib.oracleFluidNew.argtypes = [C.c_float, C.c_float, C.c_float, C.c_double]
+        lib.oracleFluidNew.restype = vp
+        lib.oracleFluidAdvance.argtypes = [vp, C.c_double]
+        lib.oracleFluidRead.argtypes = [vp, vp]
+        lib.oracleFluidRead.restype = C.c_double
+        lib.oracleFluidFree.argtypes = [vp]
         _oracle = lib
     return _oracle
+
+
+class Fluid:
+    """The disc fluid of the oracle (prefix "oracle") or of the reference itself (prefix "ref"): made,
+    advanced, read (the field as float32 and the moment it is of), freed."""
+
+    def __init__(self, lib, prefix: str, inner: float, outer: float, spin: float, time: float):
+        self.lib, self.prefix = lib, prefix
+        self.handle = getattr(lib, prefix + "FluidNew")(inner, outer, spin, time)
+        if not self.handle:
+            raise RuntimeError("fluid allocation failed")
+
+    def advance(self, time: float) -> bool:
+        return bool(getattr(self.lib, self.prefix + "FluidAdvance")(self.handle, time))
+
+    def read(self):
+        out = np.empty(FLUID_FLOATS, np.float32)
+        t = getattr(self.lib, self.prefix + "FluidRead")(self.handle, out.ctypes.data)
+        return out, t
+
+    def free(self):
+        if self.handle:
+            getattr(self.lib, self.prefix + "FluidFree")(self.handle)
+            self.handle = None
 
 
 def _ptr(a: np.ndarray | None):
@@ -143,5 +173,11 @@ def ref() -> C.CDLL:
         lib.refOrbitSpeed.restype = C.c_float
         lib.refPoolThreads.argtypes = [C.c_int]
         lib.refPoolThreads.restype = C.c_int
+        lib.refFluidNew.argtypes = [C.c_float, C.c_float, C.c_float, C.c_double]
+        lib.refFluidNew.restype = vp
+        lib.refFluidAdvance.argtypes = [vp, C.c_double]
+        lib.refFluidRead.argtypes = [vp, vp]
+        lib.refFluidRead.restype = C.c_double
+        lib.refFluidFree.argtypes = [vp]
         _ref = lib
     return _ref

@@ -80,4 +80,12 @@ void oracleJitter(uint32_t seed, uint32_t pixel, uint32_t k, float* dx, float* d
 /* The bloom pyramid and tone map of a frame's light (width * height * 4 floats) to BGRA (postOracle.c). */
 void oraclePost(const OracleFrame* h, const float* hdr, uint32_t* bgra);
 
+/* The disc fluid (fluidOracle.c, after src/scene/fluid.c): made for a disc and a moment, advanced to a
+ * later moment in steps of 0.2 (returns whether it stepped), its field (1024 x 256 floats) and moment. */
+typedef struct OracleFluid OracleFluid;
+OracleFluid* oracleFluidNew(float inner, float outer, float spin, double time);
+int oracleFluidAdvance(OracleFluid* f, double time);
+double oracleFluidRead(const OracleFluid* f, float* out);
+void oracleFluidFree(OracleFluid* f);
+
 #endif

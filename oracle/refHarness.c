@@ -56,6 +56,15 @@ double refFluid(const RefView* v, float* out) {
     return artfFluidTime(s->hole.fluid);
 }
 
+/* The reference's disc fluid by itself (fluid.c:255-336): made, advanced, read, freed. */
+void* refFluidNew(float inner, float outer, float spin, double time) { return artfFluidNew(inner, outer, spin, time); }
+int refFluidAdvance(void* f, double time) { return artfFluidAdvance((ArtfFluid*)f, time); }
+double refFluidRead(const void* f, float* out) {
+    memcpy(out, artfFluidField((const ArtfFluid*)f), sizeof(float) * ARTF_FLUID_WIDTH * ARTF_FLUID_HEIGHT);
+    return artfFluidTime((const ArtfFluid*)f);
+}
+void refFluidFree(void* f) { artfFluidFree((ArtfFluid*)f); }
+
 /* n rays at image positions (nx, ny) in -1..1 and moments time[]: linear RGB of each, 3 floats a ray. */
 void refTrace(const ArtfHoleFrame* h, const float* map, const float* fluid, int n, const float* nx, const float* ny,
               const float* time, float* rgb) {

@@ -65,6 +65,15 @@ def draw_cases():
             ("odd_3x2", g["odd_3x2"], 4.5, 1.0), ("spinless_3x3_bloom", g["spinless_3x3"], 3.0, 2.0)]
 
 
+def fluid_cases():
+    """Discs whose fluid is recorded (name, spin, start time, the moments it is advanced to in turn): the
+    inner edge at the ISCO, the outer at 12.  The moments cover a step, several, the 48-step cap, a clock
+    behind the gas (no step) and one set far back (the gas restarts its clock there)."""
+    return [("a0.9", 0.9, 0.0, [1.0, 3.05, 20.0, 19.9, 5.0, 6.0]),
+            ("a0.998", 0.998, 7.0, [7.8, 10.0, 27.0]),
+            ("a-0.5", -0.5, 0.0, [0.6])]
+
+
 def main():
     if not binding.ref_available():
         sys.exit("the reference is not built: make -f oracle/ref.mk")
@@ -164,6 +173,22 @@ def main():
         if bgra.size <= 40000:
             arrays[f"draw_{name}"] = bgra
         print("draw", name, sha(bgra)[:16])
+
+    # the reference's disc fluid (fluid.c): its field's bytes after its start and after each advance
+    out["fluid"] = {}
+    for name, spin, t0, times in fluid_cases():
+        inner = float(lib.artfCudaIsco(spin))
+        fl = binding.Fluid(ref, "ref", inner, 12.0, spin, t0)
+        field, t = fl.read()
+        states = [{"advance_to": None, "stepped": None, "time": t, "field_sha256": sha(field)}]
+        arrays[f"fluid_{name}_row100"] = field.reshape(256, 1024)[100].copy()
+        for target in times:
+            stepped = fl.advance(target)
+            field, t = fl.read()
+            states.append({"advance_to": target, "stepped": stepped, "time": t, "field_sha256": sha(field)})
+        fl.free()
+        out["fluid"][name] = {"inner": inner, "outer": 12.0, "spin": spin, "time": t0, "states": states}
+        print("fluid", name, [s["field_sha256"][:12] for s in states])
 
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
