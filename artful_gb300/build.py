@@ -36,6 +36,7 @@ UNITS = {
     "lensTangent.cu": [],
     "lensAdjoint.cu": FAST,
     "fluid.cu": EXACT,
+    "disc.cu": EXACT,
 }
 C_UNITS = ["holeHost.c", "renderer.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]

@@ -161,6 +161,10 @@ SIGNATURES = {
     "artfCudaHoleTangents": (C.c_int, [_vp, P(HoleParams), P(HoleFrame), P(HoleFrame64), _vp, _vp, _vp, _vp]),
     "artfCudaHoleAdjoint": (C.c_int, [_vp, P(HoleParams), C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp,
                                       _vp, P(AdjointResult), P(TraceStats)]),
+    # the reference's painted disc, made on the GPU
+    "artfCudaPaintDisc": (C.c_int, [_vp, _vp, C.c_float, C.c_float, C.c_float]),
+    "artfCudaHoleRings": (None, [_vp, _vp, C.c_float, C.c_float, C.c_float]),
+    "artfCudaHoleColours": (None, [_vp]),
     # the disc's fluid on the GPU
     "artfCudaFluidNew": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_double, P(_vp)]),
     "artfCudaFluidAdvance": (C.c_int, [_vp, C.c_double, P(C.c_int)]),

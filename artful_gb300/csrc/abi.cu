@@ -622,6 +622,15 @@ int contextStream(ArtfCuda* ctx, cudaStream_t* stream) {
     *stream = ctx->stream;
     return ARTF_CUDA_OK;
 }
+/* The context's map, about to be written on the device (disc.cu): held from now on, under version 0 so
+ * that the next artfCudaSetMap copies whatever it is given. */
+int contextMap(ArtfCuda* ctx, float** map) {
+    if (int s = enter(ctx)) return s;
+    *map = ctx->map;
+    ctx->mapHeld = true;
+    ctx->mapVersion = 0;
+    return ARTF_CUDA_OK;
+}
 int checkTraceFrame(const ArtfCudaHoleFrame* frame, const ArtfCudaTraceOptions* options) {
     return checkFrame(frame, options);
 }

@@ -328,8 +328,7 @@ static float rowRadius(float rho, float inner, float outer) { return inner / (1.
 #define DISC_KELVIN 4500.f  /* the disc's one temperature (the reference's HOLE_KELVIN) */
 #define TABLE_KELVIN 6500.0 /* heat 1 is this; the colour table's middle */
 
-static void ringSpeedHeat(float* map, float inner, float outer, float spin) {
-    float* rows = map + ARTF_CUDA_ROWS_AT;
+static void ringSpeedHeatRows(float* rows, float inner, float outer, float spin) {
     for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
         const float r = rowRadius((float)y / (float)(ARTF_CUDA_MAP_HEIGHT - 1), inner, outer);
         rows[y * 2] = 1.f / (6.2831853f * (r * sqrtf(r) + spin));
@@ -337,14 +336,21 @@ static void ringSpeedHeat(float* map, float inner, float outer, float spin) {
     }
 }
 
-void artfCudaSetRings(float* map, float inner, float outer, float spin) {
-    ringSpeedHeat(map, inner, outer, spin);
-    float* glow = map + ARTF_CUDA_GLOW_AT;
+static void ringSpeedHeat(float* map, float inner, float outer, float spin) {
+    ringSpeedHeatRows(map + ARTF_CUDA_ROWS_AT, inner, outer, spin);
+}
+
+void artfCudaHoleRings(float* rows, float* glow, float inner, float outer, float spin) {
+    ringSpeedHeatRows(rows, inner, outer, spin);
     for (int y = 0; y < ARTF_CUDA_MAP_HEIGHT; ++y) {
         const float r = rowRadius((float)y / (float)(ARTF_CUDA_MAP_HEIGHT - 1), inner, outer);
         const float out = r / inner;
         glow[y] = 6.f * out * sqrtf(out);
     }
+}
+
+void artfCudaSetRings(float* map, float inner, float outer, float spin) {
+    artfCudaHoleRings(map + ARTF_CUDA_ROWS_AT, map + ARTF_CUDA_GLOW_AT, inner, outer, spin);
 }
 
 /* e^x as (1 + x / 2^20)^(2^20): multiplications only (the reference's exactExp). */
@@ -377,8 +383,9 @@ static void blackBodyRgb(double kelvin, float* rgb) {
     for (int c = 0; c < 3; ++c) rgb[c] = (float)(v[c] / most);
 }
 
-static void colourTable(float* map) {
-    float* colors = map + ARTF_CUDA_COLORS_AT;
+static void colourTable(float* map) { artfCudaHoleColours(map + ARTF_CUDA_COLORS_AT); }
+
+void artfCudaHoleColours(float* colors) {
     for (int i = 0; i < ARTF_CUDA_COLORS; ++i) {
         /* (through float, as the reference's artfMaxf takes it) */
         const double kelvin = fmaxRef((float)(TABLE_KELVIN * (double)i / (ARTF_CUDA_COLORS / 2)), 400.f);

@@ -418,12 +418,13 @@ def main():
 
     cpu = None
     batch = None
-    adjoint = fitting = None
+    adjoint = fitting = next_rows = None
     if rank == 0 and not args.quick:
         cpu = cpu_baseline(scene, frame, map_, fluid, rays)
         batch = batch_measurement(lib, ctx, args.steps, flush)
         adjoint = adjoint_measurement(lib, ctx, args.steps, flush)
         fitting = fit_measurement(lib, ctx, args.fd_fits)
+        next_rows = next_rows_measurement(lib, ctx)
 
     lib.artfCudaDestroy(ctx)
     if rank != 0:
@@ -460,6 +461,8 @@ def main():
         line["adjoint"] = adjoint
     if fitting:
         line["inverse_fit"] = fitting
+    if next_rows:
+        line["disc_inputs"] = next_rows
     print(json.dumps(line), flush=True)
 
 
@@ -528,6 +531,54 @@ def adjoint_measurement(lib, ctx, steps, flush):
                             "forward_fp32_1448x816_ms": ms_fp32_big,
                             "adjoint_over_forward_fp32": ms_adj8 / ms_fp32_big},
     }
+
+
+def next_rows_measurement(lib, ctx):
+    """The disc's inputs made on the GPU, byte for byte the reference's: the painted map (hole.c
+    buildDisc + setRings) and the fluid's step (fluid.c), each beside the oracle's scalar C restatement
+    of the same code timed on one host core (the reference runs them on all cores)."""
+    import torch
+    from artful_gb300 import capi
+    from oracle import binding
+    inner, outer, spin = float(lib.artfCudaIsco(0.998)), 12.0, 0.998
+    dev = torch.empty(capi.MAP_FLOATS, dtype=torch.float32, device="cuda")
+    paint = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        capi.check(lib.artfCudaPaintDisc(ctx, dev.data_ptr(), inner, outer, spin))  # (synchronous)
+        paint.append((time.perf_counter() - t0) * 1e3)
+    fluid = C.c_void_p()
+    t0 = time.perf_counter()
+    capi.check(lib.artfCudaFluidNew(ctx, inner, outer, spin, 0.0, C.byref(fluid)))
+    fluid_new_ms = (time.perf_counter() - t0) * 1e3
+    stream = torch.cuda.ExternalStream(lib.artfCudaStream(ctx))
+    steps = {}
+    for n in (1, 48):
+        times = []
+        for _ in range(5):
+            start_t = lib.artfCudaFluidTime(fluid)
+            begin, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            begin.record(stream)
+            capi.check(lib.artfCudaFluidAdvance(fluid, start_t + n * 0.2 + 1e-3, None))
+            end.record(stream)
+            end.synchronize()
+            times.append(begin.elapsed_time(end))
+        steps[n] = statistics.median(times) / n
+    lib.artfCudaFluidFree(fluid)
+    orc = binding.oracle()
+    host = np.zeros(capi.MAP_FLOATS, np.float32)
+    t0 = time.perf_counter()
+    orc.oraclePaintDisc(host.ctypes.data)
+    oracle_paint_ms = (time.perf_counter() - t0) * 1e3
+    fl = binding.Fluid(orc, "oracle", inner, outer, spin, 0.0)
+    t0 = time.perf_counter()
+    fl.advance(48 * 0.2 + 1e-3)
+    oracle_step_ms = (time.perf_counter() - t0) * 1e3 / 48
+    fl.free()
+    return {"paint_disc_ms": statistics.median(paint), "fluid_new_ms": fluid_new_ms,
+            "fluid_step_ms": steps[1], "fluid_step_ms_in_48": steps[48],
+            "cpu_baseline": {"paint_disc_ms": oracle_paint_ms, "fluid_step_ms": oracle_step_ms, "cores": 1,
+                             "kind": "port", "sample": "one painted map; 48 fluid steps"}}
 
 
 def fit_measurement(lib, ctx, fd_fits):

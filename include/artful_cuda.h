@@ -125,6 +125,10 @@ int artfCudaHoleFrame64(const ArtfCudaCamera* camera, const ArtfCudaBlackHoleDes
                         int width, int height, ArtfCudaHoleFrame64* out);
 /* hole.c:186 setRings: per map row its orbit speed and heat, and its glow (the reference's painted disc). */
 void artfCudaSetRings(float* map, float inner, float outer, float spin);
+/* The same tables by themselves: rows (ARTF_CUDA_MAP_HEIGHT x 2) and glow (ARTF_CUDA_MAP_HEIGHT). */
+void artfCudaHoleRings(float* rows, float* glow, float inner, float outer, float spin);
+/* hole.c:161-166: the black-body colour table (ARTF_CUDA_COLORS x 3 floats). */
+void artfCudaHoleColours(float* colors);
 
 /* The synthetic disc and sky of the benchmark configurations, written into a whole map.
  *   gas:   value noise on a 64 x 64 lattice in (radius row, azimuth), seeded, in [0.5, 1.5];
@@ -385,6 +389,14 @@ typedef struct ArtfCudaAdjointResult {
 int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
                         const float* map, const float* fluid, const float* targets, int checkpointEvery, float* hdr,
                         float* pixelGrads, ArtfCudaAdjointResult* results, ArtfCudaTraceStats* stats);
+
+/* ---- the reference's painted disc, made on the GPU (src/scene/hole.c:136-197) ----------------------- */
+
+/* buildDisc then setRings: the map Artful draws a hole with (gas strands and clouds, dust lanes, the
+ * sky's dust band, black-body colours, the rings' tables for a disc from inner to outer around a hole of
+ * this spin), byte for byte the reference's, into a device map of ARTF_CUDA_MAP_FLOATS (NULL: the
+ * context's, which the trace then reads).  The reference paints it on the CPU at start-up.  Synchronous. */
+int artfCudaPaintDisc(ArtfCuda* ctx, float* map, float inner, float outer, float spin);
 
 /* ---- the disc's gas, stepped on the GPU (src/scene/fluid.c) --------------------------------------- */
 

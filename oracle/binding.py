@@ -64,6 +64,8 @@ def oracle() -> C.CDLL:
         lib.oracleFluidRead.argtypes = [vp, vp]
         lib.oracleFluidRead.restype = C.c_double
         lib.oracleFluidFree.argtypes = [vp]
+        lib.oraclePaintDisc.argtypes = [vp]
+        lib.oracleSetRings.argtypes = [vp, C.c_float, C.c_float, C.c_float]
         _oracle = lib
     return _oracle
 

@@ -88,4 +88,9 @@ int oracleFluidAdvance(OracleFluid* f, double time);
 double oracleFluidRead(const OracleFluid* f, float* out);
 void oracleFluidFree(OracleFluid* f);
 
+/* The reference's painted disc (discOracle.c, after hole.c:136-178 buildDisc): gas, dust, colours and
+ * sky into a whole map (ring tables left as they are); and the ring tables for a disc (hole.c:186). */
+void oraclePaintDisc(float* map);
+void oracleSetRings(float* map, float inner, float outer, float spin);
+
 #endif

@@ -174,6 +174,18 @@ def main():
             arrays[f"draw_{name}"] = bgra
         print("draw", name, sha(bgra)[:16])
 
+    # the reference's painted disc map (hole.c:136-197 buildDisc and setRings) for some discs
+    out["painted"] = {}
+    for name in ("c1", "retro_edge", "spinless_3x3"):
+        view = scenes.golden_scenes()[name]
+        v = RefView(view.camera, view.desc, view.width, view.height)
+        frame, clamped = ref_frame(ref, view)
+        painted = np.zeros(capi.MAP_FLOATS, np.float32)
+        ref.refMap(C.byref(v), painted.ctypes.data)
+        out["painted"][name] = {"inner": float(clamped.discInner), "outer": float(clamped.discOuter),
+                                "spin": float(clamped.spin), "map_sha256": sha(painted)}
+        print("painted", name, sha(painted)[:16])
+
     # the reference's disc fluid (fluid.c): its field's bytes after its start and after each advance
     out["fluid"] = {}
     for name, spin, t0, times in fluid_cases():
