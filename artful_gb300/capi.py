@@ -69,7 +69,7 @@ class TraceOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("jitter", C.c_int), ("seed", C.c_uint32), ("stepScale", C.c_float),
                 ("horizonBand", C.c_float), ("blockSize", C.c_int), ("compactEvery", C.c_int),
                 ("persistent", C.c_int), ("guards", C.c_uint32), ("fp64Batch", C.c_int),
-                ("refillBatch", C.c_int)]
+                ("refillBatch", C.c_int), ("bandRays", C.c_int64)]
 
 
 GUARD_MOTION, GUARD_HORIZON, GUARD_RADIAL, GUARD_POLAR, GUARD_PSI, GUARD_ALL = 1, 2, 4, 8, 16, 31
@@ -84,7 +84,8 @@ class RayEnd(C.Structure):
 class TraceStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("steps", C.c_uint64), ("crossings", C.c_uint64), ("escapes", C.c_uint64),
                 ("fp64Steps", C.c_uint64), ("fp64Horizon", C.c_uint64), ("fp64Radial", C.c_uint64),
-                ("fp64Polar", C.c_uint64), ("fp64Rounds", C.c_uint64), ("flops", C.c_double), ("ms", C.c_float)]
+                ("fp64Polar", C.c_uint64), ("fp64Rounds", C.c_uint64), ("flops", C.c_double), ("ms", C.c_float),
+                ("bands", C.c_uint32)]
 
 
 class View(C.Structure):

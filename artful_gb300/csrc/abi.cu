@@ -67,6 +67,7 @@ struct ArtfCuda {
     double* adjResults;
     double* adjResultsHost;
     size_t adjResultViews;
+    uint32_t lastBands; /* launches of the last trace (1 but for a frame in bands) */
     int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
     bool lost;
 };
@@ -341,15 +342,23 @@ static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precisio
     stats->flops = artfFlops(stats->rays, stats->steps, stats->crossings, stats->escapes, frame.spin[0] != 0.f,
                              frame.look[1] != 0.f, frame.look[2] > 0.f);
     stats->ms = ms;
+    stats->bands = ctx->lastBands;
     return ARTF_CUDA_OK;
 }
 
-/* One frame (or ray list) of any precision: the launch, bracketed by events, and the stats. */
-static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCudaTraceStats* stats) {
-    if (int s = spendLaunch(ctx)) return s;
+/* Frames that go out in bands (vulkan.c:1733-1734): above this many rays, bands of that many. */
+static const int64_t kRaysApart = 64000000, kRaysABand = 8000000;
+
+/* One launch of the frame's tile rows l.tileRowBegin .. + l.tileRows (all when 0 rows), or of its ray
+ * list, in the given precision. */
+static int launchBand(ArtfCuda* ctx, artf::TraceLaunch& l, int precision) {
     if (precision == ARTF_CUDA_MIXED) {
         if (int s = reserveTable(ctx, 1)) return s;
-        const size_t pixels = (size_t)l.frame.size[0] * l.frame.size[1];
+        const int height = (int)l.frame.size[1];
+        const int rowBegin = l.tileRows > 0 ? l.tileRowBegin * 4 : 0;
+        const int rows = l.tileRows > 0 ? (rowBegin + l.tileRows * 4 < height ? l.tileRows * 4 : height - rowBegin)
+                                        : height;
+        const size_t pixels = (size_t)l.frame.size[0] * rows;
         const size_t np = l.rayCount > 0 ? 0 : artf::mixedRayPlanes(l, l.frame);
         if (np)
             if (int s = reservePlanes(ctx, pixels * np)) return s;
@@ -357,22 +366,54 @@ static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, ArtfCuda
         const int units = artf::mixedFillView(l, l.frame, l.frame64, l.map, l.fluid, l.hdr, l.ends,
                                               np ? ctx->planes : nullptr, 0, ctx->stage);
         if (int s = sendTable(ctx, 1)) return s;
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
         const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "mixed trace launch: %s", cudaGetErrorString(e));
-    } else {
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
-        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-        cudaError_t e = cudaSuccess;
-        switch (precision) {
-        case ARTF_CUDA_EXACT: e = artf::launchExact(l); break;
-        case ARTF_CUDA_FP32: e = artf::launchFast(l); break;
-        default: e = artf::launchFp64(l); break;
-        }
-        if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "trace launch: %s", cudaGetErrorString(e));
+        return ARTF_CUDA_OK;
     }
+    cudaError_t e = cudaSuccess;
+    switch (precision) {
+    case ARTF_CUDA_EXACT: e = artf::launchExact(l); break;
+    case ARTF_CUDA_FP32: e = artf::launchFast(l); break;
+    default: e = artf::launchFp64(l); break;
+    }
+    if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "trace launch: %s", cudaGetErrorString(e));
+    return ARTF_CUDA_OK;
+}
+
+/* One frame (or ray list) of any precision: its launches (a band of whole tile rows each, waited for,
+ * when the frame has more rays than bandRays allows: ArtfCudaTraceOptions), bracketed by events, and
+ * the stats.  Every pixel's rays are traced within one band, so the bands change when, not what. */
+static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, int64_t bandRays, ArtfCudaTraceStats* stats) {
+    if (int s = spendLaunch(ctx)) return s;
+    const int tileRows = ((int)l.frame.size[1] + 3) / 4;
+    const int64_t perPixel = l.jitter ? l.jitter : (int64_t)l.frame.size[2] * l.frame.size[2];
+    const int64_t total = (int64_t)l.frame.size[0] * l.frame.size[1] * perPixel;
+    const int64_t perTileRow = (int64_t)l.frame.size[0] * 4 * perPixel;
+    int64_t band = 0;
+    if (l.rayCount == 0 && bandRays == 0 && total > kRaysApart) band = kRaysABand;
+    if (l.rayCount == 0 && bandRays > 0 && total > bandRays) band = bandRays;
+    const int rowsABand = band > 0 ? (int)(band / perTileRow > 1 ? band / perTileRow : 1) : tileRows;
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
+    int bands = 0, status = ARTF_CUDA_OK;
+    for (int first = 0; first < tileRows && !status; first += rowsABand) {
+        if (band > 0) {
+            l.tileRowBegin = first;
+            l.tileRows = rowsABand < tileRows - first ? rowsABand : tileRows - first;
+            if (bands > 0) { /* each band its own launch, waited for (vulkan.c:1740-1754) */
+                CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+                CUDA_OR(ARTF_CUDA_ELAUNCH,
+                        cudaMemsetAsync(ctx->counters + artf::CQueue, 0, sizeof(unsigned long long), ctx->stream));
+            }
+        }
+        status = launchBand(ctx, l, precision);
+        ++bands;
+        if (l.rayCount > 0) break;
+    }
+    l.tileRowBegin = l.tileRows = 0;
+    if (status) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    ctx->lastBands = (uint32_t)bands;
     return stats ? readStats(ctx, l.frame, precision, stats) : ARTF_CUDA_OK;
 }
 
@@ -401,7 +442,7 @@ extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* fra
     l.jitter = 0;
     l.rayCount = n;
     l.rayX = nx, l.rayY = ny, l.rayTime = time, l.rayRgb = rgb;
-    return runTrace(ctx, l, precision, stats);
+    return runTrace(ctx, l, precision, -1, stats);
 }
 
 extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
@@ -421,7 +462,7 @@ extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, 
     l.fluid = fluid ? fluid : ctx->fluid;
     l.hdr = (float4*)hdr;
     l.ends = ends;
-    return runTrace(ctx, l, options->precision, stats);
+    return runTrace(ctx, l, options->precision, options->bandRays, stats);
 }
 
 extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
@@ -486,7 +527,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
     l.fluid = ctx->fluid;
     l.hdr = ctx->hdr;
     /* trace (its own events), then the pyramid and tone map, timed from the trace's start */
-    if ((status = runTrace(ctx, l, options->precision, nullptr))) return status;
+    if ((status = runTrace(ctx, l, options->precision, options->bandRays, nullptr))) return status;
     float* planes[3] = {ctx->bloom, ctx->bloom + bloomPixels, ctx->bloom + 2 * bloomPixels};
     if ((status = artfCudaPostLaunch(frame, (const float*)ctx->hdr, planes, ctx->bgra, ctx->stream)))
         return fail(status, "bloom and tone map launch: %s", cudaGetErrorString(cudaGetLastError()));
@@ -609,6 +650,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
         stats->crossings = c[artf::CCrossings];
         stats->escapes = c[artf::CEscapes];
         stats->ms = ms;
+        stats->bands = 1;
     }
     return ARTF_CUDA_OK;
 }
@@ -666,6 +708,7 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    ctx->lastBands = 1;
     return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
 }
 
@@ -767,6 +810,7 @@ extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* st
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaGraphLaunch(g->exec, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
+    ctx->lastBands = 1;
     return stats ? readStats(ctx, g->first, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
 }
 

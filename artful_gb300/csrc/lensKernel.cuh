@@ -28,7 +28,8 @@ template <typename R> struct KernelParams {
     int maxSteps;
     int rays;
     float share;
-    int tilesX, tiles;          /* 8 x 4 pixel tiles */
+    int tilesX, tiles;          /* 8 x 4 pixel tiles: this launch's count */
+    int tileBegin;              /* the first (a band of the frame starts further down) */
 };
 
 /* What a thread counts, reduced over the warp before it reaches the device counters. */
@@ -145,9 +146,9 @@ template <typename R> __device__ __forceinline__ void tracePixel(const KernelPar
 /* One warp per 8 x 4 tile, one thread per pixel. */
 template <typename R> __global__ void __launch_bounds__(256) traceTiles(const KernelParams<R> p) {
     const int lane = threadIdx.x & 31;
-    const int tile = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int local = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), tile = p.tileBegin + local;
     Tally t;
-    if (tile < p.tiles) {
+    if (local < p.tiles) {
         const int32_t x = (tile % p.tilesX) * 8 + (lane & 7), y = (tile / p.tilesX) * 4 + (lane >> 3);
         if (x < p.f.width && y < p.f.height) tracePixel(p, x, y, t);
     }
@@ -159,10 +160,11 @@ template <typename R> __global__ void __launch_bounds__(256) traceQueue(const Ke
     const int lane = threadIdx.x & 31;
     Tally t;
     for (;;) {
-        int tile = 0;
-        if (lane == 0) tile = (int)atomicAdd(p.counters + CQueue, 1ull);
-        tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-        if (tile >= p.tiles) break;
+        int local = 0;
+        if (lane == 0) local = (int)atomicAdd(p.counters + CQueue, 1ull);
+        local = __shfl_sync(0xFFFFFFFFu, local, 0);
+        if (local >= p.tiles) break;
+        const int tile = p.tileBegin + local;
         const int32_t x = (tile % p.tilesX) * 8 + (lane & 7), y = (tile / p.tilesX) * 4 + (lane >> 3);
         if (x < p.f.width && y < p.f.height) tracePixel(p, x, y, t);
         __syncwarp();
@@ -207,7 +209,11 @@ template <typename R> cudaError_t launchUniform(const TraceLaunch& l, const void
     p.rays = l.jitter ? l.jitter : (int)(l.frame.size[2] * l.frame.size[2]);
     p.share = l.jitter ? 1.f / (float)l.jitter : l.frame.image[3];
     p.tilesX = ((int)l.frame.size[0] + 7) / 8;
-    p.tiles = p.tilesX * (((int)l.frame.size[1] + 3) / 4);
+    const int tileRows = ((int)l.frame.size[1] + 3) / 4;
+    const int bandBegin = l.tileRows > 0 ? l.tileRowBegin : 0;
+    const int bandRows = l.tileRows > 0 ? l.tileRows : tileRows;
+    p.tileBegin = bandBegin * p.tilesX;
+    p.tiles = p.tilesX * bandRows;
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
         const RayList list = {l.rayCount, l.rayX, l.rayY, l.rayTime, l.rayRgb};

@@ -35,6 +35,9 @@ struct TraceLaunch {
     int refillBatch;
     int smCount;
     cudaStream_t stream;
+    /* a band of the frame: 4-pixel tile rows [tileRowBegin, tileRowBegin + tileRows); 0 rows: all */
+    int tileRowBegin;
+    int tileRows;
     /* a list of rays in place of a frame's pixels (rayCount > 0) */
     int rayCount;
     const float* rayX;

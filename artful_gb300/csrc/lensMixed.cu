@@ -48,6 +48,7 @@ struct MixedView {
     float4* rayOut;
     float rhoScale, uGuard, share;
     int tilesX, pixelUnits, units, unitBase, rays, jitter;
+    int rowBegin, rows; /* the pixel rows this launch traces (a band of the frame, or all of it) */
     uint32_t seed;
 };
 static_assert(sizeof(MixedView) <= kMixedViewBytesMax, "a view table slot outgrew kMixedViewBytesMax");
@@ -318,10 +319,10 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                         local -= plane * v->pixelUnits;
                         const int tile = local >> 5, within = local & 31;
                         x = (tile % v->tilesX) * 8 + (within & 7);
-                        y = (tile / v->tilesX) * 4 + (within >> 3);
+                        y = v->rowBegin + (tile / v->tilesX) * 4 + (within >> 3);
                         k = plane;
                         kEnd = v->rayOut ? plane + 1 : v->rays;
-                        if (x >= v->f.width || y >= v->f.height) k = kEnd; /* (off the image: fetch again) */
+                        if (x >= v->f.width || y >= v->rowBegin + v->rows) k = kEnd; /* (off the band: fetch again) */
                     }
                 }
             }
@@ -379,8 +380,10 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                 const unsigned rayBits = classBits(mixedFinish(r, ended, end, t));
                 live = false;
                 if (v->rayOut) {
-                    const size_t plane = (size_t)v->f.width * (size_t)v->f.height;
-                    v->rayOut[(size_t)k * plane + index] = make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
+                    /* (a plane holds the band's pixels) */
+                    const size_t plane = (size_t)v->f.width * (size_t)v->rows;
+                    const size_t inBand = (size_t)(y - v->rowBegin) * (size_t)v->f.width + (size_t)x;
+                    v->rayOut[(size_t)k * plane + inBand] = make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
                     ++k;
                 } else {
                     bits |= rayBits;
@@ -401,7 +404,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
 __global__ void __launch_bounds__(256) mixedCombine(const MixedView* views) {
     const MixedView& v = views[blockIdx.y];
     if (!v.rayOut) return;
-    const size_t pixels = (size_t)v.f.width * (size_t)v.f.height;
+    const size_t pixels = (size_t)v.f.width * (size_t)v.rows; /* the band's */
     const size_t i = (size_t)blockIdx.x * 256 + threadIdx.x;
     if (i >= pixels) return;
     float sum[3] = {0.f, 0.f, 0.f};
@@ -411,7 +414,8 @@ __global__ void __launch_bounds__(256) mixedCombine(const MixedView* views) {
         sum[0] = sum[0] + q.x, sum[1] = sum[1] + q.y, sum[2] = sum[2] + q.z;
         bits |= (unsigned)q.w;
     }
-    v.hdr[i] = make_float4(sum[0] * v.share, sum[1] * v.share, sum[2] * v.share, (float)bits);
+    v.hdr[(size_t)v.rowBegin * (size_t)v.f.width + i] =
+        make_float4(sum[0] * v.share, sum[1] * v.share, sum[2] * v.share, (float)bits);
 }
 
 /* The per-ray entry point: rays at given image positions in the table's first view. */
@@ -468,7 +472,11 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.jitter = l.jitter;
     v.seed = l.seed;
     v.tilesX = ((int)frame.size[0] + 7) / 8;
-    v.pixelUnits = v.tilesX * (((int)frame.size[1] + 3) / 4) * 32;
+    const int tileRows = ((int)frame.size[1] + 3) / 4;
+    const int bandBegin = l.tileRows > 0 ? l.tileRowBegin : 0, bandRows = l.tileRows > 0 ? l.tileRows : tileRows;
+    v.rowBegin = bandBegin * 4;
+    v.rows = (bandBegin + bandRows) * 4 < (int)frame.size[1] ? bandRows * 4 : (int)frame.size[1] - v.rowBegin;
+    v.pixelUnits = v.tilesX * bandRows * 32;
     v.rayOut = v.rays > 1 ? rayOut : nullptr; /* (one ray a pixel: the pixel is the ray) */
     v.units = v.pixelUnits * (v.rayOut ? v.rays : 1);
     v.unitBase = unitBase;

@@ -56,7 +56,7 @@ cudaError_t launchTangents(const TraceLaunch& l, const double* jacobian, double 
     p.maxSteps = 192;
     p.rays = 1;
     p.share = 1.f;
-    p.tilesX = p.tiles = 0;
+    p.tilesX = p.tiles = p.tileBegin = 0;
     const int pixels = (int)(l.frame.size[0] * l.frame.size[1]);
     traceTangents<<<(pixels + 63) / 64, 64, 0, l.stream>>>(p, out);
     return cudaGetLastError();

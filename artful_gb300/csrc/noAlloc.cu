@@ -138,6 +138,7 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
         stats->fp64Radial = c[artf::CFp64Radial];
         stats->fp64Polar = c[artf::CFp64Polar];
         stats->fp64Rounds = c[artf::CFp64Rounds];
+        stats->bands = 1;
     }
     return ARTF_CUDA_OK;
 }

@@ -194,6 +194,11 @@ typedef struct ArtfCudaTraceOptions {
     uint32_t guards;     /* mixed: which FP64 guards run (ARTF_CUDA_GUARD_*); 0 means all */
     int fp64Batch;       /* mixed: lanes that wait for an FP64 sub-step before a warp runs them; 0: 32 */
     int refillBatch;     /* mixed: idle lanes before a warp starts new rays (FP64 set-ups); 0: 32 */
+    int64_t bandRays;    /* a frame of more rays than this goes out in bands of whole rows of at most this
+                          * many rays, each launched and waited for, so that no launch holds the GPU long
+                          * (vulkan.c:1729-1756).  0: the reference's choice, bands of 8e6 rays for frames
+                          * above 6.4e7 (a 4K frame of 64 rays a pixel is seconds of work); < 0: never.
+                          * Single frames only; the result is the same bits either way */
 } ArtfCudaTraceOptions;
 
 /* The mixed trace's FP64 guards. */
@@ -236,6 +241,7 @@ typedef struct ArtfCudaTraceStats {
     uint64_t fp64Rounds;                         /* mixed: warp rounds of FP64 steps */
     double flops;        /* algorithmic FP32-pipe operations (the counting rule is in lensFlops.h) */
     float ms;            /* device time of the trace kernel(s), CUDA events on the context's stream */
+    uint32_t bands;      /* launches the frame went out in (ArtfCudaTraceOptions.bandRays) */
 } ArtfCudaTraceStats;
 
 /* Traces one frame into `hdr` (device memory, width * height float4: linear RGB and the class bits).
