@@ -173,7 +173,11 @@ SIGNATURES = {
     "artfCudaFluidTime": (C.c_double, [_vp]),
     "artfCudaFluidRead": (C.c_int, [_vp, _vp]),
     "artfCudaFluidFree": (None, [_vp]),
+    "artfCudaFluidClock": (C.c_int, [P(C.c_double), C.c_double]),
+    "artfCudaFluidStep": (C.c_int, [_vp, C.c_int64, C.c_double]),
+    "artfCudaUseFluid": (C.c_int, [_vp, _vp]),
     # the renderer backend (artful_cuda_renderer.h)
+    "artfCudaRendererSetDeviceInputs": (None, [_vp, C.c_bool]),
     "artfCudaNew": (_vp, [_vp]),
     "artfCudaNewWithReader": (_vp, [_vp, _vp]),
     "artfCudaRendererReadLight": (C.c_bool, [_vp, _vp]),
@@ -209,6 +213,14 @@ class FrameStats(C.Structure):
 class Overlay(C.Structure):
     _fields_ = [("pixels", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("stride", C.c_int),
                 ("partial", C.c_bool), ("damage", C.c_void_p), ("damageCount", C.c_size_t)]
+
+
+class HoleInputs(C.Structure):
+    """What a renderer reads of a scene (artful_cuda_renderer.h ArtfCudaHoleInputs)."""
+    _fields_ = [("on", C.c_bool), ("camera", Camera), ("desc", BlackHoleDesc), ("map", C.c_void_p),
+                ("mapVersion", C.c_uint64), ("fluid", C.c_void_p), ("fluidVersion", C.c_uint64),
+                ("fluidTime", C.c_double), ("gasGeneration", C.c_uint64), ("gasStart", C.c_double),
+                ("gasSteps", C.c_uint64), ("gasClock", C.c_double)]
 
 
 class RendererVtbl(C.Structure):

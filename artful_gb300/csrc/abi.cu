@@ -179,6 +179,21 @@ extern "C" int artfCudaSetFluid(ArtfCuda* ctx, const float* hostFluid, uint64_t 
     return upload(ctx, ctx->fluid, hostFluid, ARTF_CUDA_FLUID_FLOATS, version, &ctx->fluidVersion, &ctx->fluidHeld);
 }
 
+/* A host map and fluid for a draw, each copied when its version changed; NULL: the context's own. */
+static int hostInputs(ArtfCuda* ctx, const float* hostMap, uint64_t mapVersion, const float* hostFluid,
+                      uint64_t fluidVersion) {
+    if (!hostMap && !ctx->mapHeld) return fail(ARTF_CUDA_EINVAL, "no map: pass one or paint the context's");
+    if (!hostFluid && !ctx->fluidHeld) return fail(ARTF_CUDA_EINVAL, "no fluid: pass one or give the context one");
+    if (hostMap)
+        if (int s = upload(ctx, ctx->map, hostMap, ARTF_CUDA_MAP_FLOATS, mapVersion, &ctx->mapVersion, &ctx->mapHeld))
+            return s;
+    if (hostFluid)
+        if (int s = upload(ctx, ctx->fluid, hostFluid, ARTF_CUDA_FLUID_FLOATS, fluidVersion, &ctx->fluidVersion,
+                           &ctx->fluidHeld))
+            return s;
+    return ARTF_CUDA_OK;
+}
+
 extern "C" const float* artfCudaDeviceMap(const ArtfCuda* ctx) { return ctx ? ctx->map : nullptr; }
 extern "C" const float* artfCudaDeviceFluid(const ArtfCuda* ctx) { return ctx ? ctx->fluid : nullptr; }
 extern "C" void* artfCudaStream(const ArtfCuda* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
@@ -473,8 +488,7 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
     if (!hostHdr) return fail(ARTF_CUDA_EINVAL, "hostHdr is NULL");
-    if ((status = artfCudaSetMap(ctx, hostMap, mapVersion))) return status;
-    if ((status = artfCudaSetFluid(ctx, hostFluid, fluidVersion))) return status;
+    if ((status = hostInputs(ctx, hostMap, mapVersion, hostFluid, fluidVersion))) return status;
     const size_t pixels = (size_t)frame->size[0] * frame->size[1];
     if (pixels > ctx->hdrPixels) {
         cudaFree(ctx->hdr);
@@ -509,8 +523,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
-    if ((status = artfCudaSetMap(ctx, hostMap, mapVersion))) return status;
-    if ((status = artfCudaSetFluid(ctx, hostFluid, fluidVersion))) return status;
+    if ((status = hostInputs(ctx, hostMap, mapVersion, hostFluid, fluidVersion))) return status;
     const size_t pixels = (size_t)frame->size[0] * frame->size[1];
     size_t bloomPixels = 0;
     for (uint32_t i = 0; i < frame->size[3] && i < ARTF_CUDA_BLOOM_LEVELS; ++i)
@@ -671,6 +684,14 @@ int contextMap(ArtfCuda* ctx, float** map) {
     *map = ctx->map;
     ctx->mapHeld = true;
     ctx->mapVersion = 0;
+    return ARTF_CUDA_OK;
+}
+/* The same for the context's fluid (fluid.cu). */
+int contextFluid(ArtfCuda* ctx, float** fluid) {
+    if (int s = enter(ctx)) return s;
+    *fluid = ctx->fluid;
+    ctx->fluidHeld = true;
+    ctx->fluidVersion = 0;
     return ARTF_CUDA_OK;
 }
 int checkTraceFrame(const ArtfCudaHoleFrame* frame, const ArtfCudaTraceOptions* options) {

@@ -26,6 +26,7 @@
 
 namespace artf {
 int contextStream(ArtfCuda* ctx, cudaStream_t* stream);
+int contextFluid(ArtfCuda* ctx, float** fluid);
 int failWith(int status, const char* message);
 }  // namespace artf
 
@@ -340,7 +341,6 @@ int advanceSteps(ArtfCudaFluid* f, int extra, int steps) {
                                              f->radial[cur], f->orbital[cur], f->rings);
         balance<<<FH, 256, 0, f->stream>>>(f->dens[cur]);
         e = cudaGetLastError();
-        f->time += DT;
     }
     if (e == cudaSuccess) {
         showField<<<blocks, 256, 0, f->stream>>>(f->dens[cur], f->field, f->rings);
@@ -424,18 +424,35 @@ extern "C" int artfCudaFluidAdvance(ArtfCudaFluid* f, double time, int* stepped)
     if (!f || !isfinite(time)) return artf::failWith(ARTF_CUDA_EINVAL, "no fluid, or a time that is not finite");
     cudaStream_t stream = nullptr;
     if (int s = artf::contextStream(f->ctx, &stream)) return s;
-    if (time - f->time < DT) {
-        /* behind: the gas does not run back, but a clock set far back starts it from there */
-        if (time < f->time - 8.0) f->time = time;
-        return ARTF_CUDA_OK;
+    double clock = f->time;
+    const int steps = artfCudaFluidClock(&clock, time);
+    if (steps > 0)
+        if (int s = advanceSteps(f, 0, steps)) return s;
+    f->time = clock;
+    if (stepped) *stepped = steps > 0;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaFluidStep(ArtfCudaFluid* f, int64_t steps, double time) {
+    if (!f || steps < 0 || !isfinite(time)) return artf::failWith(ARTF_CUDA_EINVAL, "fluid step: no fluid, or bad steps or time");
+    cudaStream_t stream = nullptr;
+    if (int s = artf::contextStream(f->ctx, &stream)) return s;
+    /* in runs of at most 4 x 48 steps, so that the eddy staging stays small */
+    for (int64_t done = 0; done < steps;) {
+        const int run = (int)(steps - done < 4 * MAX_STEPS ? steps - done : 4 * MAX_STEPS);
+        if (int s = advanceSteps(f, 0, run)) return s;
+        done += run;
     }
-    int steps = (int)((time - f->time) / DT);
-    if (steps > MAX_STEPS) {
-        f->time = time - (double)MAX_STEPS * DT;
-        steps = MAX_STEPS;
-    }
-    if (int s = advanceSteps(f, 0, steps)) return s;
-    if (stepped) *stepped = 1;
+    f->time = time;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaUseFluid(ArtfCuda* ctx, const ArtfCudaFluid* f) {
+    if (!f || f->ctx != ctx) return artf::failWith(ARTF_CUDA_EINVAL, "use fluid: no fluid, or one of another context");
+    float* dst = nullptr;
+    if (int s = artf::contextFluid(ctx, &dst)) return s;
+    const cudaError_t e = cudaMemcpyAsync(dst, f->field, sizeof(float) * FIELD, cudaMemcpyDeviceToDevice, f->stream);
+    if (e != cudaSuccess) return artf::failWith(ARTF_CUDA_ELAUNCH, cudaGetErrorString(e));
     return ARTF_CUDA_OK;
 }
 

@@ -393,6 +393,27 @@ void artfCudaHoleColours(float* colors) {
     }
 }
 
+/* ---- the gas's clock (src/scene/fluid.c:319-333, and its step's f->time += STEP at fluid.c:240) ------ */
+
+#define FLUID_STEP .2f     /* a step's time, in float as the reference's STEP */
+#define FLUID_MOST_STEPS 48
+
+int artfCudaFluidClock(double* clock, double time) {
+    if (!clock || !isfinite(time)) return 0;
+    if (time - *clock < FLUID_STEP) {
+        /* behind: no step; a clock set more than 8 back restarts the gas's clock there */
+        if (time < *clock - 8.0) *clock = time;
+        return 0;
+    }
+    int steps = (int)((time - *clock) / FLUID_STEP);
+    if (steps > FLUID_MOST_STEPS) {
+        *clock = time - (double)FLUID_MOST_STEPS * FLUID_STEP;
+        steps = FLUID_MOST_STEPS;
+    }
+    for (int i = 0; i < steps; ++i) *clock += FLUID_STEP;
+    return steps;
+}
+
 /* ---- deterministic elementary functions (double, IEEE + - * / only) ------------------------------ */
 
 #define LN2 0.6931471805599453

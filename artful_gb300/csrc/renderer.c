@@ -31,6 +31,9 @@ struct ArtfCudaScene {
     bool ownMap;                /* the caller's map, not the synthetic one */
     uint64_t seed;
     float emissivity;
+    uint32_t gasGeneration;     /* the gas's clock, kept as artfSceneSetBlackHole keeps its fluid's */
+    double gasStart, gasClock;
+    uint64_t gasSteps;
 };
 
 static uint64_t nextSceneId = 1;
@@ -98,6 +101,14 @@ void artfCudaSceneSetBlackHole(ArtfCudaScene* s, const ArtfCudaBlackHoleDesc* de
         artfCudaSynthMap(&synth, s->map);
         ++s->mapVersion;
     }
+    /* hole.c:264-270: a new gas for a new disc or spin, else the old one advanced to the time */
+    if (!sameSpin) {
+        ++s->gasGeneration;
+        s->gasStart = s->gasClock = d.time;
+        s->gasSteps = 0;
+    } else {
+        s->gasSteps += (uint64_t)artfCudaFluidClock(&s->gasClock, d.time);
+    }
 }
 
 void artfCudaSceneSetHoleMap(ArtfCudaScene* s, const float* map, const float* fluid, double fluidTime) {
@@ -125,6 +136,10 @@ bool artfCudaSceneReadHole(const void* scene, ArtfCudaHoleInputs* out) {
     out->fluid = s->fluid;
     out->fluidVersion = s->id << 32 | (s->fluidVersion & 0xFFFFFFFFu);
     out->fluidTime = s->fluidTime;
+    out->gasGeneration = s->id << 32 | s->gasGeneration;
+    out->gasStart = s->gasStart;
+    out->gasSteps = s->gasSteps;
+    out->gasClock = s->gasClock;
     return true;
 }
 
@@ -142,6 +157,12 @@ typedef struct CudaRenderer {
     int overlayWidth, overlayHeight;
     char description[160];
     ArtfCudaFrameStats stats;
+    bool deviceInputs;
+    bool painted;               /* the context's map is the painted disc of paintedDisc (inner, outer, spin) */
+    float paintedDisc[3];
+    ArtfCudaFluid* gas;         /* the scene's gas, on the device */
+    bool gasShown;              /* the context's fluid is the gas's field */
+    uint64_t gasGeneration, gasSteps;
 } CudaRenderer;
 
 static double nowMs(void) {
@@ -214,6 +235,52 @@ static void composite(CudaRenderer* c) {
         }
 }
 
+/* The scene's painted map and gas made on the device, as hole.c:249-270 makes them on the host: the map
+ * painted again when the disc or the spin changes; the gas started afresh when the scene's starts
+ * afresh, else stepped as many steps as the scene's clock has counted since the last draw.  A reader
+ * that knows no clock (gasGeneration 0) gets the reference's rule applied at each draw instead.  Returns
+ * an ArtfCuda status; *fluidTime: the gas's time. */
+static int deviceInputs(CudaRenderer* c, const ArtfCudaHoleInputs* in, double* fluidTime) {
+    const ArtfCudaBlackHoleDesc* d = &in->desc;
+    const bool sameDisc = c->painted && c->paintedDisc[0] == d->discInner && c->paintedDisc[1] == d->discOuter;
+    const bool sameSpin = sameDisc && c->paintedDisc[2] == d->spin;
+    int status;
+    if (!sameSpin) {
+        c->painted = false;
+        if ((status = artfCudaPaintDisc(c->ctx, NULL, d->discInner, d->discOuter, d->spin))) return status;
+        c->paintedDisc[0] = d->discInner, c->paintedDisc[1] = d->discOuter, c->paintedDisc[2] = d->spin;
+        c->painted = true;
+    }
+    const bool known = in->gasGeneration != 0;
+    const bool restart = !c->gas || (known ? in->gasGeneration != c->gasGeneration || in->gasSteps < c->gasSteps
+                                           : !sameSpin);
+    bool changed = restart || !c->gasShown;
+    if (restart) {
+        artfCudaFluidFree(c->gas);
+        c->gas = NULL;
+        if ((status = artfCudaFluidNew(c->ctx, d->discInner, d->discOuter, d->spin, known ? in->gasStart : d->time,
+                                       &c->gas)))
+            return status;
+        c->gasGeneration = in->gasGeneration;
+        c->gasSteps = 0;
+    }
+    if (known) {
+        const uint64_t steps = in->gasSteps - c->gasSteps;
+        if ((status = artfCudaFluidStep(c->gas, (int64_t)steps, in->gasClock))) return status;
+        c->gasSteps = in->gasSteps;
+        changed = changed || steps > 0;
+    } else if (!restart) {
+        int stepped = 0;
+        if ((status = artfCudaFluidAdvance(c->gas, d->time, &stepped))) return status;
+        changed = changed || stepped;
+    }
+    c->gasShown = false;
+    if (changed && (status = artfCudaUseFluid(c->ctx, c->gas))) return status;
+    c->gasShown = true;
+    *fluidTime = artfCudaFluidTime(c->gas);
+    return ARTF_CUDA_OK;
+}
+
 static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
     CudaRenderer* c = (CudaRenderer*)r;
     const double t0 = nowMs();
@@ -226,10 +293,16 @@ static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
         c->stats.cpuMs = nowMs() - t0;
         return true;
     }
+    double fluidTime = in.fluidTime;
+    if (c->deviceInputs) {
+        if (deviceInputs(c, &in, &fluidTime)) return false;
+    } else {
+        c->painted = c->gasShown = false; /* (the context's map and fluid are the host's from here on) */
+    }
     ArtfCudaHoleFrame frame;
     ArtfCudaHoleFrame64 frame64;
-    if (!artfCudaHoleFrame(&in.camera, &in.desc, in.fluidTime, c->width, c->height, &frame) ||
-        artfCudaHoleFrame64(&in.camera, &in.desc, in.fluidTime, c->width, c->height, &frame64))
+    if (!artfCudaHoleFrame(&in.camera, &in.desc, fluidTime, c->width, c->height, &frame) ||
+        artfCudaHoleFrame64(&in.camera, &in.desc, fluidTime, c->width, c->height, &frame64))
         return true; /* (nothing to draw at this size; the device is fine) */
     ArtfCudaTraceOptions options;
     memset(&options, 0, sizeof options);
@@ -237,8 +310,11 @@ static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
     options.stepScale = 1.f;
     options.persistent = 1;
     ArtfCudaTraceStats stats;
-    const int status = artfCudaHoleDraw(c->ctx, &frame, &frame64, in.map, in.mapVersion, in.fluid, in.fluidVersion,
-                                        &options, c->light, c->bgra, &stats);
+    const int status = c->deviceInputs
+                           ? artfCudaHoleDraw(c->ctx, &frame, &frame64, NULL, 0, NULL, 0, &options, c->light, c->bgra,
+                                              &stats)
+                           : artfCudaHoleDraw(c->ctx, &frame, &frame64, in.map, in.mapVersion, in.fluid,
+                                              in.fluidVersion, &options, c->light, c->bgra, &stats);
     if (status) return false; /* the device is lost (or unusable): the renderer must be freed */
     composite(c);
     c->stats.lensMs = stats.ms;
@@ -266,6 +342,7 @@ static void cudaStats(const ArtfCudaRenderer* r, ArtfCudaFrameStats* out) {
 
 static void cudaDestroy(ArtfCudaRenderer* r) {
     CudaRenderer* c = (CudaRenderer*)r;
+    artfCudaFluidFree(c->gas);
     artfCudaDestroy(c->ctx);
     free(c->bgra);
     free(c->light);
@@ -311,3 +388,7 @@ void artfCudaRendererSetPrecision(ArtfCudaRenderer* r, int precision) {
 }
 
 ArtfCuda* artfCudaRendererContext(ArtfCudaRenderer* r) { return r ? ((CudaRenderer*)r)->ctx : NULL; }
+
+void artfCudaRendererSetDeviceInputs(ArtfCudaRenderer* r, bool on) {
+    if (r) ((CudaRenderer*)r)->deviceInputs = on;
+}

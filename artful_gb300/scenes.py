@@ -129,6 +129,24 @@ def config4_start() -> Scene:
                  emissivity=2.7)
 
 
+def timeline():
+    """A hole over time as an application animates one: its description set every frame, a frame drawn
+    after most.  The gas takes single steps, two settings come between two draws, a jump hits the 48-step
+    cap, the clock falls behind the gas and then far back (the gas's clock restarts there), the spin
+    changes (the disc repainted, a new gas), then the disc, then both come back, and the camera moves.
+    Returns (width, height, [(camera, clamped-before description, draw after it)])."""
+    def at(t, spin=0.9, outer=12.0, bloom=4.5):
+        d = hole_desc(spin, outer=outer, time=t)
+        d.bloom = bloom
+        return d
+    near, far = camera(80.0, 30.0), camera(72.0, 34.0)
+    steps = [(near, at(0.0), True), (near, at(0.1), True), (near, at(1.05), False), (near, at(2.3), True),
+             (near, at(30.0), True), (near, at(29.0), True), (near, at(5.0), True), (near, at(5.5), True),
+             (near, at(6.0, spin=0.6), True), (near, at(6.4, spin=0.6, outer=16.0), True),
+             (near, at(7.0), True), (far, at(7.3), True), (far, at(7.35), False), (far, at(9.0), True)]
+    return 160, 90, steps
+
+
 def golden_scenes():
     """The views whose reference outputs are recorded in tests/golden/."""
     c1 = config1()

@@ -264,7 +264,8 @@ int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const A
  * and the tone map with its dither (src/software/software.c:320-427, src/software/lens.inc:387-440) to
  * premultiplied BGRA (alpha 255).  Copies back the linear light (width * height float4) to hostHdr and
  * the BGRA frame (width * height uint32) to hostBgra, each when not NULL.  Synchronous.  stats->ms is
- * the device time of trace and bloom together (the reference's lensMs). */
+ * the device time of trace and bloom together (the reference's lensMs).  A NULL hostMap or hostFluid
+ * draws with what the context holds (artfCudaPaintDisc, artfCudaUseFluid, an earlier upload). */
 int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
                      const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                      const ArtfCudaTraceOptions* options, float* hostHdr, uint32_t* hostBgra,
@@ -333,8 +334,8 @@ typedef struct ArtfCudaTuning {
 int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options,
                      ArtfCudaTuning* result);
 
-/* The same from host memory to host memory: copies the map and fluid (when their versions changed),
- * traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */
+/* The same from host memory to host memory: copies the map and fluid (when their versions changed; NULL:
+ * the context's own), traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */
 int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
                        const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                        const ArtfCudaTraceOptions* options, float* hostHdr, ArtfCudaTraceStats* stats);
@@ -416,6 +417,17 @@ int artfCudaFluidNew(ArtfCuda* ctx, float inner, float outer, float spin, double
 /* fluid.c:319 artfFluidAdvance: steps of 0.2 up to `time`, at most 48 a call (the gas does not run back);
  * *stepped (may be NULL): whether the field changed.  On the context's stream. */
 int artfCudaFluidAdvance(ArtfCudaFluid* f, double time, int* stepped);
+/* The clock of fluid.c:319-333 alone, on the host: how many steps artfFluidAdvance takes from a gas whose
+ * time is *clock towards `time`, with *clock moved to the gas's time after them (a step adds 0.2f).  The
+ * field after any run of advances depends only on the steps taken since its start, so a caller that
+ * counts them can bring a gas up to date later in one call (artfCudaFluidStep). */
+int artfCudaFluidClock(double* clock, double time);
+/* `steps` steps now (any number), the field after them, and the gas's time set to `time`.  On the
+ * context's stream. */
+int artfCudaFluidStep(ArtfCudaFluid* f, int64_t steps, double time);
+/* The field copied into the context's fluid (on the device, on its stream), which traces and draws with
+ * no fluid given then read.  f must be of this context. */
+int artfCudaUseFluid(ArtfCuda* ctx, const ArtfCudaFluid* f);
 /* fluid.c:335-336: the field (device, ARTF_CUDA_FLUID_FLOATS, owned by f; valid after the stream's work)
  * and the moment it is of. */
 const float* artfCudaFluidField(const ArtfCudaFluid* f);

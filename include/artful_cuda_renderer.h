@@ -95,6 +95,14 @@ typedef struct ArtfCudaHoleInputs {
     const float* fluid;         /* ARTF_CUDA_FLUID_FLOATS, host, borrowed */
     uint64_t fluidVersion;
     double fluidTime;           /* the moment the fluid field is of */
+    /* The scene's gas by its clock, for a backend that steps the gas on the device
+     * (artfCudaRendererSetDeviceInputs): a number that changes whenever the gas starts afresh (hole.c:265,
+     * a new disc or spin; 0: not known, and the backend then follows desc.time at each draw), the moment
+     * it started, the steps taken since (artfCudaFluidClock's count over every advance) and its clock. */
+    uint64_t gasGeneration;
+    double gasStart;
+    uint64_t gasSteps;
+    double gasClock;
 } ArtfCudaHoleInputs;
 
 typedef bool (*ArtfCudaSceneReader)(const void* scene, ArtfCudaHoleInputs* out);
@@ -110,6 +118,12 @@ ArtfCudaRenderer* artfCudaNewWithReader(const ArtfCudaRendererOptions* options, 
 bool artfCudaRendererReadLight(ArtfCudaRenderer* r, float* dst);
 void artfCudaRendererSetPrecision(ArtfCudaRenderer* r, int precision);
 ArtfCuda* artfCudaRendererContext(ArtfCudaRenderer* r);
+/* Device inputs: the renderer ignores the scene's host map and fluid and makes the reference's own on
+ * the GPU from the description, as artfSceneSetBlackHole makes them on the CPU (hole.c:249-270): the
+ * painted disc (artfCudaPaintDisc) whenever the disc or the spin changes, and the gas (ArtfCudaFluid),
+ * started then and stepped as the scene's clock says (the inputs' gas fields).  No map or fluid crosses
+ * from the host.  Off by default (the scene's host inputs are drawn). */
+void artfCudaRendererSetDeviceInputs(ArtfCudaRenderer* r, bool on);
 
 /* ---- the library's own minimal hole scene (Artful's scene API for this path, restated) ------------ */
 
@@ -120,7 +134,9 @@ void artfCudaSceneFree(ArtfCudaScene* s);
 void artfCudaSceneSetCamera(ArtfCudaScene* s, const ArtfCudaCamera* camera);
 /* scene.h:500 artfSceneSetBlackHole: NULL removes the hole.  The description is clamped as the
  * reference clamps it; the disc is the synthetic one (artfCudaSynthMap: seed, emissivity 3), rebuilt when
- * the disc or the spin changes; the fluid field is 1 everywhere. */
+ * the disc or the spin changes; the fluid field is 1 everywhere.  The gas's clock runs as the
+ * reference's (a new gas when the disc or the spin changes, else an advance to the description's time),
+ * for renderers that draw with device inputs. */
 void artfCudaSceneSetBlackHole(ArtfCudaScene* s, const ArtfCudaBlackHoleDesc* desc);
 /* A caller's own map and fluid field in place of the synthetic ones (copied). */
 void artfCudaSceneSetHoleMap(ArtfCudaScene* s, const float* map, const float* fluid, double fluidTime);

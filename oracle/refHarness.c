@@ -167,6 +167,32 @@ void refDraw(const RefView* v, const float* map, const float* fluid, int threads
     artfSceneFree(s);
 }
 
+/* The reference's own scene over time: one scene and one software renderer of the first view's size;
+ * each view's camera and description set in turn (artfSceneSetBlackHole paints the disc, starts and
+ * advances the gas: hole.c:242-271), and after each view marked in `drawAfter` a frame drawn and read
+ * into the next width * height of bgra; the gas's time after each view into fluidTimes (may be NULL).
+ * Nothing is put in place of the scene's own map or fluid. */
+void refDrawScene(const RefView* views, const int* drawAfter, int count, int threads, uint32_t* bgra,
+                  double* fluidTimes) {
+    ArtfScene* s = artfSceneNew();
+    ArtfRendererOptions o = artfRendererDefaults(views[0].width, views[0].height);
+    o.backend = ARTF_BACKEND_SOFTWARE;
+    o.threads = threads;
+    ArtfRenderer* r = artfRendererNew(&o);
+    const size_t pixels = (size_t)views[0].width * (size_t)views[0].height;
+    for (int i = 0; i < count; ++i) {
+        artfSceneSetCamera(s, &views[i].camera);
+        artfSceneSetBlackHole(s, &views[i].desc);
+        if (fluidTimes) fluidTimes[i] = artfFluidTime(s->hole.fluid);
+        if (!drawAfter[i]) continue;
+        artfRendererDraw(r, s);
+        artfRendererReadPixels(r, bgra);
+        bgra += pixels;
+    }
+    artfRendererFree(r);
+    artfSceneFree(s);
+}
+
 /* The reference's ISCO and orbit speed (hole.c:207, hole.c:215). */
 float refIsco(float spin) { return artfHoleIsco(spin); }
 float refOrbitSpeed(float spin, float r) { return artfBlackHoleOrbitSpeed(spin, r); }

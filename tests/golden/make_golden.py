@@ -202,6 +202,20 @@ def main():
         out["fluid"][name] = {"inner": inner, "outer": 12.0, "spin": spin, "time": t0, "states": states}
         print("fluid", name, [s["field_sha256"][:12] for s in states])
 
+    # the reference's own scene over time (hole.c:242-271: its painted disc, its gas started and advanced
+    # by artfSceneSetBlackHole), drawn by its software renderer after the marked settings
+    ref.refDrawScene.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    width, height, steps = scenes.timeline()
+    views = (RefView * len(steps))(*[RefView(cam, d, width, height) for cam, d, _ in steps])
+    marks = np.array([int(draw) for _, _, draw in steps], np.int32)
+    frames = np.zeros((int(marks.sum()), height, width), np.uint32)
+    times = np.zeros(len(steps), np.float64)
+    ref.refDrawScene(views, marks.ctypes.data, len(steps), 0, frames.ctypes.data, times.ctypes.data)
+    out["timeline"] = {"width": width, "height": height, "fluid_times": times.tolist(),
+                       "bgra_sha256": [sha(f) for f in frames]}
+    arrays["timeline_last"] = frames[-1]
+    print("timeline", [sha(f)[:8] for f in frames])
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1)

@@ -121,3 +121,30 @@ def test_trace_reads_the_field_on_the_device(lib, ctx):
     np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
     assert (field != 1.0).any()  # (a real field, not the unit one)
     fl.free()
+
+
+def test_counted_steps_equal_the_advances(lib, ctx):
+    """The field depends only on the steps taken since the start: a gas advanced call by call and one
+    stepped once by the count artfCudaFluidClock gives (more than one call's 48) hold the same bytes and
+    the same time.  (That the trace reads a gas handed to the context is the renderer's timeline test.)"""
+    inner, outer, spin = float(lib.artfCudaIsco(0.9)), 12.0, 0.9
+    a = GpuFluid(lib, ctx, inner, outer, spin, 2.0)
+    b = GpuFluid(lib, ctx, inner, outer, spin, 2.0)
+    clock, total = C.c_double(2.0), 0
+    try:
+        for target in (2.7, 3.1, 12.0, 11.0, 16.05):
+            a.advance(target)
+            total += lib.artfCudaFluidClock(C.byref(clock), target)
+        assert total > 48
+        capi.check(lib.artfCudaFluidStep(b.handle, total, clock.value))
+        fa, ta = a.read()
+        fb, tb = b.read()
+        assert ta == tb == clock.value
+        assert _sha(fa) == _sha(fb)
+        capi.check(lib.artfCudaUseFluid(ctx, b.handle))
+        capi.check(lib.artfCudaSetFluid(ctx, scenes.unit_fluid().ctypes.data, 0))  # (as other tests left it)
+        assert lib.artfCudaUseFluid(ctx, None) != 0
+        assert lib.artfCudaFluidStep(b.handle, -1, 1.0) != 0
+    finally:
+        a.free()
+        b.free()

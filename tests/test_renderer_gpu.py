@@ -175,3 +175,64 @@ def test_backend_mixed_precision_stays_within_tolerance(lib, golden):
     finally:
         r.free()
         lib.artfCudaSceneFree(s)
+
+
+def test_backend_draws_the_reference_scene_over_time(lib, golden):
+    """Device inputs: the reference's own scene (its painted disc, its gas started and advanced by
+    artfSceneSetBlackHole, hole.c:242-271) drawn by the reference's software renderer over a timeline,
+    against this backend painting the disc and stepping the gas on the GPU from the same settings: every
+    frame the same bytes.  A second renderer that joins halfway catches the gas up in one call and draws the
+    same; switching device inputs off and on again redraws the same."""
+    meta, arrays = golden
+    want = meta["timeline"]["bgra_sha256"]
+    width, height, steps = scenes.timeline()
+    r = Backend(lib, width, height)
+    lib.artfCudaRendererSetDeviceInputs(r.ptr, True)
+    late = None
+    s = lib.artfCudaSceneNew()
+    try:
+        drawn = 0
+        for i, (cam, desc, draw) in enumerate(steps):
+            lib.artfCudaSceneSetCamera(s, C.byref(cam))
+            lib.artfCudaSceneSetBlackHole(s, C.byref(desc))
+            if not draw:
+                continue
+            assert r.draw(s)
+            assert hashlib.sha256(r.read().tobytes()).hexdigest() == want[drawn], (i, drawn)
+            if drawn == 5:   # after the clock ran far back: a new renderer, a gas 23 steps on
+                late = Backend(lib, width, height)
+                lib.artfCudaRendererSetDeviceInputs(late.ptr, True)
+            if late is not None:
+                assert late.draw(s)
+                assert hashlib.sha256(late.read().tobytes()).hexdigest() == want[drawn], ("late", i)
+            drawn += 1
+        assert drawn == len(want)
+        assert np.array_equal(r.read(), arrays["timeline_last"])
+        # host inputs (the scene's synthetic map) in between, then device inputs again: the same frame
+        lib.artfCudaRendererSetDeviceInputs(r.ptr, False)
+        assert r.draw(s)
+        assert not np.array_equal(r.read(), arrays["timeline_last"])
+        lib.artfCudaRendererSetDeviceInputs(r.ptr, True)
+        assert r.draw(s)
+        assert np.array_equal(r.read(), arrays["timeline_last"])
+    finally:
+        r.free()
+        if late is not None:
+            late.free()
+        lib.artfCudaSceneFree(s)
+
+
+def test_draw_with_what_the_context_holds(lib, ctx, golden):
+    """artfCudaHoleDraw with no host map or fluid draws the context's: uploaded once, then drawn again."""
+    meta, _ = golden
+    view = _draw_case("c1_bloom")
+    frame, frame64, clamped = scenes.frame(view)
+    m = scenes.synth_map(lib, clamped, view.seed, view.emissivity)
+    fluid = scenes.unit_fluid()
+    capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
+    capi.check(lib.artfCudaSetFluid(ctx, fluid.ctypes.data, 0))
+    opts = capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 1)
+    bgra = np.zeros((view.height, view.width), np.uint32)
+    capi.check(lib.artfCudaHoleDraw(ctx, C.byref(frame), C.byref(frame64), None, 0, None, 0, C.byref(opts), None,
+                                    bgra.ctypes.data, None))
+    assert hashlib.sha256(bgra.tobytes()).hexdigest() == meta["draw"]["c1_bloom"]["bgra_sha256"]
