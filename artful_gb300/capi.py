@@ -69,9 +69,10 @@ class TraceOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("jitter", C.c_int), ("seed", C.c_uint32), ("stepScale", C.c_float),
                 ("horizonBand", C.c_float), ("blockSize", C.c_int), ("compactEvery", C.c_int),
                 ("persistent", C.c_int), ("guards", C.c_uint32), ("fp64Batch", C.c_int),
-                ("refillBatch", C.c_int), ("bandRays", C.c_int64)]
+                ("refillBatch", C.c_int), ("bandRays", C.c_int64), ("order", C.c_int)]
 
 
+ORDER_HEAVY_FIRST, ORDER_PIXELS = 0, 1
 GUARD_MOTION, GUARD_HORIZON, GUARD_RADIAL, GUARD_POLAR, GUARD_PSI, GUARD_ALL = 1, 2, 4, 8, 16, 31
 
 

@@ -58,6 +58,9 @@ struct ArtfCuda {
     /* the mixed trace's ray planes (one float4 a ray of a pixel), for views of several rays a pixel */
     float4* planes;
     size_t planeCount;
+    /* the mixed trace's heavy-first order (artf::mixedOrderBytes) */
+    void* order;
+    size_t orderBytes;
     /* the adjoint's view table (device and pinned staging), block sums and per-view results */
     void* adjTable;
     void* adjStage;
@@ -145,6 +148,7 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->table);
     cudaFreeHost(ctx->stage);
     cudaFree(ctx->planes);
+    cudaFree(ctx->order);
     cudaFree(ctx->adjTable);
     cudaFreeHost(ctx->adjStage);
     cudaFree(ctx->adjPartials);
@@ -221,6 +225,8 @@ static int checkOptions(const ArtfCudaTraceOptions* o) {
         return fail(ARTF_CUDA_EINVAL, "blockSize %d: 0, or a multiple of 32 up to 256", o->blockSize);
     if (o->compactEvery < 0 || o->compactEvery > 4096) return fail(ARTF_CUDA_EINVAL, "compactEvery out of range");
     if (o->horizonBand < 0.f || o->horizonBand > 1.f) return fail(ARTF_CUDA_EINVAL, "horizonBand out of [0, 1]");
+    if (o->order != ARTF_CUDA_ORDER_HEAVY_FIRST && o->order != ARTF_CUDA_ORDER_PIXELS)
+        return fail(ARTF_CUDA_EINVAL, "unknown order %d", o->order);
     return ARTF_CUDA_OK;
 }
 
@@ -248,6 +254,7 @@ static artf::TraceLaunch launchOf(const ArtfCuda* ctx, const ArtfCudaTraceOption
     l.guards = o->guards;
     l.fp64Batch = o->fp64Batch;
     l.refillBatch = o->refillBatch;
+    l.order = o->order;
     if (ctx->hasTuning && o->precision == ARTF_CUDA_MIXED) {
         if (!l.blockSize) l.blockSize = ctx->tuned.blockSize;
         if (!l.compactEvery) l.compactEvery = ctx->tuned.compactEvery;
@@ -295,11 +302,25 @@ static int reservePlanes(ArtfCuda* ctx, size_t count) {
     return ARTF_CUDA_OK;
 }
 
-/* Fills the staging table from views; the total queue units in *units.  planes: room for the views' ray
- * planes (planesOf), or NULL to trace a pixel a unit; *combinePixels: the largest view with planes. */
+/* The heavy-first order's scratch for this many tiles and units. */
+static int reserveOrder(ArtfCuda* ctx, int tiles, int units) {
+    const size_t bytes = artf::mixedOrderBytes(tiles, units);
+    if (bytes <= ctx->orderBytes) return ARTF_CUDA_OK;
+    cudaFree(ctx->order); /* (synchronises: no launch still reads the old order) */
+    ctx->order = nullptr;
+    ctx->orderBytes = 0;
+    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->order, bytes));
+    ctx->orderBytes = bytes;
+    return ARTF_CUDA_OK;
+}
+
+/* Fills the staging table from views; the total queue units in *units and tiles in *tiles.  planes: room
+ * for the views' ray planes (planesOf), or NULL to trace a pixel a unit; *combinePixels: the largest view
+ * with planes. */
 static int fillTable(ArtfCuda* ctx, const artf::TraceLaunch& l, const ArtfCudaView* views, int count,
-                     const ArtfCudaTraceOptions* o, void* stage, float4* planes, int* units, size_t* combinePixels) {
-    long long total = 0;
+                     const ArtfCudaTraceOptions* o, void* stage, float4* planes, int* units, size_t* combinePixels,
+                     int* tiles) {
+    long long total = 0, tileTotal = 0;
     size_t offset = 0, widest = 0;
     for (int i = 0; i < count; ++i) {
         const ArtfCudaView& v = views[i];
@@ -313,13 +334,16 @@ static int fillTable(ArtfCuda* ctx, const artf::TraceLaunch& l, const ArtfCudaVi
             offset += pixels * np;
             widest = pixels > widest ? pixels : widest;
         }
+        int viewTiles = 0;
         const int n = artf::mixedFillView(l, v.frame, v.frame64, v.map ? v.map : ctx->map, v.fluid ? v.fluid : ctx->fluid,
-                                          (float4*)v.hdr, v.ends, rayOut, (int)total,
-                                          (char*)stage + artf::mixedViewBytes() * i);
+                                (float4*)v.hdr, v.ends, rayOut, (int)total, (int)tileTotal,
+                                (char*)stage + artf::mixedViewBytes() * i, &viewTiles);
         total += n;
+        tileTotal += viewTiles;
         if (total > 0x7FFFFFFFLL) return fail(ARTF_CUDA_EINVAL, "batch of %lld rays is too large", total);
     }
     *units = (int)total;
+    *tiles = (int)tileTotal;
     *combinePixels = widest;
     return ARTF_CUDA_OK;
 }
@@ -378,10 +402,12 @@ static int launchBand(ArtfCuda* ctx, artf::TraceLaunch& l, int precision) {
         if (np)
             if (int s = reservePlanes(ctx, pixels * np)) return s;
         if (int s = waitStaging(ctx)) return s;
+        int tiles = 0;
         const int units = artf::mixedFillView(l, l.frame, l.frame64, l.map, l.fluid, l.hdr, l.ends,
-                                              np ? ctx->planes : nullptr, 0, ctx->stage);
+                                              np ? ctx->planes : nullptr, 0, 0, ctx->stage, &tiles);
+        if (int s = reserveOrder(ctx, tiles, units)) return s;
         if (int s = sendTable(ctx, 1)) return s;
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0, tiles, ctx->order);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "mixed trace launch: %s", cudaGetErrorString(e));
         return ARTF_CUDA_OK;
     }
@@ -720,13 +746,15 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     if ((status = reserveTable(ctx, count))) return status;
     if ((status = reservePlanes(ctx, planesOf(l, views, count)))) return status;
     if ((status = waitStaging(ctx))) return status;
-    int units = 0;
+    int units = 0, tiles = 0;
     size_t combine = 0;
-    if ((status = fillTable(ctx, l, views, count, options, ctx->stage, ctx->planes, &units, &combine))) return status;
+    if ((status = fillTable(ctx, l, views, count, options, ctx->stage, ctx->planes, &units, &combine, &tiles)))
+        return status;
+    if ((status = reserveOrder(ctx, tiles, units))) return status;
     if ((status = sendTable(ctx, count))) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine);
+    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
@@ -735,7 +763,7 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
 
 struct ArtfCudaGraph {
     ArtfCuda* ctx;
-    int count, units;
+    int count, units, tiles;
     size_t combine;
     ArtfCudaTraceOptions options;
     ArtfCudaHoleFrame first; /* (for the stats' counting rule) */
@@ -743,6 +771,7 @@ struct ArtfCudaGraph {
     void* stage;
     float4* planes; /* the graph's own ray planes: its captured launches keep the pointer */
     size_t planeCount;
+    void* order;    /* and its own heavy-first order */
     cudaGraph_t graph;
     cudaGraphExec_t exec;
 };
@@ -756,6 +785,7 @@ extern "C" void artfCudaBatchGraphDestroy(ArtfCudaGraph* g) {
     cudaFree(g->table);
     cudaFreeHost(g->stage);
     cudaFree(g->planes);
+    cudaFree(g->order);
     free(g);
 }
 
@@ -781,15 +811,19 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
         artfCudaBatchGraphDestroy(g);
         return fail(ARTF_CUDA_ENOMEM, "graph table allocation");
     }
-    if ((status = fillTable(ctx, l, views, count, options, g->stage, g->planes, &g->units, &g->combine))) {
+    if ((status = fillTable(ctx, l, views, count, options, g->stage, g->planes, &g->units, &g->combine, &g->tiles))) {
         artfCudaBatchGraphDestroy(g);
         return status;
+    }
+    if (cudaMalloc(&g->order, artf::mixedOrderBytes(g->tiles, g->units)) != cudaSuccess) {
+        artfCudaBatchGraphDestroy(g);
+        return fail(ARTF_CUDA_ENOMEM, "graph order allocation");
     }
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaMemcpyAsync(g->table, g->stage, bytes, cudaMemcpyHostToDevice, ctx->stream);
         cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
-        artf::launchMixedTable(l, g->table, count, g->units, g->combine);
+        artf::launchMixedTable(l, g->table, count, g->units, g->combine, g->tiles, g->order);
         e = cudaStreamEndCapture(ctx->stream, &g->graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
@@ -815,8 +849,10 @@ extern "C" int artfCudaBatchGraphUpdate(ArtfCudaGraph* g, const ArtfCudaView* vi
     /* (the planes the graph holds must cover the new views: sizes may differ at equal tile counts) */
     if (planesOf(l, views, count) != g->planeCount)
         return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
-    if ((status = fillTable(g->ctx, l, views, count, &g->options, g->stage, g->planes, &units, &combine))) return status;
-    if (units != g->units || combine != g->combine)
+    int tiles = 0;
+    if ((status = fillTable(g->ctx, l, views, count, &g->options, g->stage, g->planes, &units, &combine, &tiles)))
+        return status;
+    if (units != g->units || combine != g->combine || tiles != g->tiles)
         return fail(ARTF_CUDA_EINVAL, "update changed the views' sizes; make a new graph");
     g->first = views[0].frame;
     return ARTF_CUDA_OK;
@@ -838,14 +874,14 @@ extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* st
 /* ---- the autotuner ------------------------------------------------------------------------------ */
 
 /* Median time of `repeats` launches of the batch already in the context's table. */
-static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int units, size_t combine, int repeats,
-                     float* ms) {
+static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int units, size_t combine, int tiles,
+                     int repeats, float* ms) {
     float times[8];
     for (int r = -1; r < repeats; ++r) {
         CUDA_OR(ARTF_CUDA_ELAUNCH,
                 cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "autotune launch: %s", cudaGetErrorString(e));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->stop));
@@ -874,9 +910,11 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
     if ((status = reserveTable(ctx, count))) return status;
     if ((status = reservePlanes(ctx, planesOf(l, views, count)))) return status;
     if ((status = waitStaging(ctx))) return status;
-    int units = 0;
+    int units = 0, tiles = 0;
     size_t combine = 0;
-    if ((status = fillTable(ctx, l, views, count, &o, ctx->stage, ctx->planes, &units, &combine))) return status;
+    if ((status = fillTable(ctx, l, views, count, &o, ctx->stage, ctx->planes, &units, &combine, &tiles)))
+        return status;
+    if ((status = reserveOrder(ctx, tiles, units))) return status;
     if ((status = sendTable(ctx, count))) return status;
 
     /* coordinate descent over the launch shape, from the defaults */
@@ -891,7 +929,7 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
     float bestMs = 0.f;
     int trials = 0;
     l.blockSize = best[0], l.compactEvery = best[1], l.fp64Batch = best[2], l.refillBatch = best[3];
-    if ((status = timeBatch(ctx, l, count, units, combine, repeats, &bestMs))) return status;
+    if ((status = timeBatch(ctx, l, count, units, combine, tiles, repeats, &bestMs))) return status;
     const float defaultMs = bestMs;
     ++trials;
     for (int pass = 0; pass < 2; ++pass)
@@ -902,7 +940,7 @@ extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int co
                 trial[d] = values[d][c];
                 l.blockSize = trial[0], l.compactEvery = trial[1], l.fp64Batch = trial[2], l.refillBatch = trial[3];
                 float ms = 0.f;
-                if ((status = timeBatch(ctx, l, count, units, combine, repeats, &ms))) return status;
+                if ((status = timeBatch(ctx, l, count, units, combine, tiles, repeats, &ms))) return status;
                 ++trials;
                 if (ms < bestMs * 0.99f) {
                     bestMs = ms;

@@ -33,6 +33,7 @@ struct TraceLaunch {
     uint32_t guards;
     int fp64Batch;
     int refillBatch;
+    int order;                    /* ARTF_CUDA_ORDER_* (the mixed trace's queue) */
     int smCount;
     cudaStream_t stream;
     /* a band of the frame: 4-pixel tile rows [tileRowBegin, tileRowBegin + tileRows); 0 rows: all */

@@ -47,7 +47,7 @@ struct MixedView {
      * whose rays one lane traces in turn. */
     float4* rayOut;
     float rhoScale, uGuard, share;
-    int tilesX, pixelUnits, units, unitBase, rays, jitter;
+    int tilesX, pixelUnits, units, unitBase, tileBase, rays, jitter;
     int rowBegin, rows; /* the pixel rows this launch traces (a band of the frame, or all of it) */
     uint32_t seed;
 };
@@ -59,6 +59,9 @@ struct MixedParams {
     const MixedView* views;
     int viewCount;
     int totalUnits;
+    /* the queue's slots (32 units: one ray plane of one tile) in the order handed out, each (view | plane
+     * << 12, tile); NULL: pixel order, view after view */
+    const uint2* order;
     unsigned long long* counters;
     float stepScale;
     int maxSteps;
@@ -274,6 +277,72 @@ __device__ __forceinline__ int viewOf(const MixedParams& p, int unit) {
     return lo;
 }
 
+/* ---- heavy first --------------------------------------------------------------------------------
+ * After the queue empties the persistent grid drains, and a lane that took a long ray late holds its SM
+ * while the others idle (a photon-ring ray runs to the step cap, ten times a sky ray's steps).  So the
+ * queue hands out the heaviest tiles first and leaves short rays for the end.  A tile's weight is the
+ * step count of one FP32 ray through its middle, stepped without shading (the disc is thin: it seldom
+ * ends a ray); tiles are counting-sorted by weight class, heaviest first.  The order changes when a ray
+ * is traced, never what it computes, so the frame is the same bits in any order. */
+
+constexpr int kWeightClasses = 25; /* steps / 16: the 384-step cap is class 24 */
+
+/* The view a batch-wide tile belongs to: the last whose first tile is at or below it. */
+__device__ __forceinline__ int tileView(const MixedParams& p, int tile) {
+    int lo = 0, hi = p.viewCount - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&p.views[mid].tileBase) <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* Each tile's weight class, and each class's count of queue slots (a tile has one a ray plane). */
+__global__ void __launch_bounds__(128) probeTiles(const MixedParams p, int totalTiles, int* weights,
+                                                  unsigned* classes) {
+    const int g = (int)(blockIdx.x * 128 + threadIdx.x);
+    if (g >= totalTiles) return;
+    const MixedView& v = p.views[tileView(p, g)];
+    const int tile = g - v.tileBase;
+    const int x = min((tile % v.tilesX) * 8 + 4, (int)v.f.width - 1);
+    const int y = min(v.rowBegin + (tile / v.tilesX) * 4 + 2, v.rowBegin + v.rows - 1);
+    float nx, ny, moment;
+    samplePosition(v.h, v.jitter, v.seed, x, y, 0, &nx, &ny, &moment);
+    RayConst<float> c;
+    RayState<float> s;
+    rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, p.stepScale, c, s);
+    const float a = v.f.a;
+    if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
+    int i = 0;
+    while (i < p.maxSteps) {
+        StepOut<float> o;
+        nystromStep(a, c, s, o);
+        ++i;
+        if (0.f > o.next.u || o.next.u > v.f.uHorizon) break;
+        s = o.next;
+    }
+    const int w = min(i >> 4, kWeightClasses - 1);
+    weights[g] = w;
+    atomicAdd(classes + w, v.rayOut ? (unsigned)v.rays : 1u);
+}
+
+/* Each tile's slots into the order, its planes together, heavier classes first (within a class in the
+ * order the atomics give). */
+__global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int totalTiles, const int* weights,
+                                                  const unsigned* classes, unsigned* cursors, uint2* order) {
+    const int g = (int)(blockIdx.x * 128 + threadIdx.x);
+    if (g >= totalTiles) return;
+    const int vi = tileView(p, g);
+    const MixedView& v = p.views[vi];
+    const int w = weights[g];
+    unsigned at = 0;
+    for (int c = kWeightClasses - 1; c > w; --c) at += classes[c];
+    const unsigned planes = v.rayOut ? (unsigned)v.rays : 1u;
+    at += atomicAdd(cursors + w, planes);
+    for (unsigned k = 0; k < planes; ++k) order[at + k] = make_uint2((unsigned)vi | k << 12, (unsigned)(g - v.tileBase));
+}
+
 /* The warp-scheduled trace (see the file's head). */
 __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     const unsigned full = 0xFFFFFFFFu;
@@ -312,12 +381,22 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                         exhausted = true;
                         unit = -1;
                     } else {
-                        v = p.views + viewOf(p, unit);
-                        int local = unit - v->unitBase;
-                        /* with ray planes the units run ray-major: a warp's lanes take neighbouring pixels */
-                        const int plane = v->rayOut ? local / v->pixelUnits : 0;
-                        local -= plane * v->pixelUnits;
-                        const int tile = local >> 5, within = local & 31;
+                        /* a slot of 32 units is one ray plane of one tile: a warp's lanes take
+                         * neighbouring pixels */
+                        int plane, tile;
+                        const int within = unit & 31; /* (every view's first unit is a multiple of 32) */
+                        if (p.order) {
+                            const uint2 slot = __ldg(p.order + (unit >> 5));
+                            v = p.views + (slot.x & 4095u);
+                            plane = v->rayOut ? (int)(slot.x >> 12) : 0;
+                            tile = (int)slot.y;
+                        } else {
+                            v = p.views + viewOf(p, unit);
+                            int local = unit - v->unitBase;
+                            plane = v->rayOut ? local / v->pixelUnits : 0;
+                            local -= plane * v->pixelUnits;
+                            tile = local >> 5;
+                        }
                         x = (tile % v->tilesX) * 8 + (within & 7);
                         y = v->rowBegin + (tile / v->tilesX) * 4 + (within >> 3);
                         k = plane;
@@ -446,6 +525,7 @@ MixedParams paramsOf(const TraceLaunch& l, const void* deviceTable, int viewCoun
     p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 32;
     p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 32;
     p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
+    p.order = nullptr;
     return p;
 }
 
@@ -455,7 +535,7 @@ size_t mixedViewBytes() { return sizeof(MixedView); }
 
 int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
                   const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, float4* rayOut, int unitBase,
-                  void* slot) {
+                  int tileBase, void* slot, int* tiles) {
     MixedView v;
     memset(&v, 0, sizeof v);
     v.f.load(frame64, frame);
@@ -480,8 +560,18 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.rayOut = v.rays > 1 ? rayOut : nullptr; /* (one ray a pixel: the pixel is the ray) */
     v.units = v.pixelUnits * (v.rayOut ? v.rays : 1);
     v.unitBase = unitBase;
+    v.tileBase = tileBase;
     memcpy(slot, &v, sizeof v);
+    *tiles = v.tilesX * bandRows;
     return v.units;
+}
+
+/* The heavy-first scratch: the weight classes' counts and cursors, a weight a tile, a slot a 32 units. */
+constexpr size_t kOrderHead = 2 * 32 * sizeof(unsigned);
+
+size_t mixedOrderBytes(int totalTiles, int totalUnits) {
+    const size_t weights = ((size_t)totalTiles * sizeof(int) + 15) & ~(size_t)15;
+    return kOrderHead + weights + (size_t)(totalUnits / 32) * sizeof(uint2);
 }
 
 int mixedGrid(const TraceLaunch& l, int totalUnits) {
@@ -494,13 +584,25 @@ int mixedGrid(const TraceLaunch& l, int totalUnits) {
 }
 
 cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits,
-                             size_t combinePixels) {
-    const MixedParams p = paramsOf(l, deviceTable, viewCount, totalUnits);
+                             size_t combinePixels, int totalTiles, void* orderScratch) {
+    MixedParams p = paramsOf(l, deviceTable, viewCount, totalUnits);
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
         traceMixedList<<<(l.rayCount + 127) / 128, 128, 0, l.stream>>>(p, l.rayCount, l.rayX, l.rayY, l.rayTime,
                                                                        l.rayRgb);
         return cudaGetLastError();
+    }
+    if (orderScratch && l.order == ARTF_CUDA_ORDER_HEAVY_FIRST && totalTiles > 0) {
+        unsigned* classes = (unsigned*)orderScratch;
+        unsigned* cursors = classes + 32;
+        int* weights = (int*)((char*)orderScratch + kOrderHead);
+        uint2* order = (uint2*)((char*)weights + (((size_t)totalTiles * sizeof(int) + 15) & ~(size_t)15));
+        const cudaError_t e = cudaMemsetAsync(orderScratch, 0, kOrderHead, l.stream);
+        if (e != cudaSuccess) return e;
+        const unsigned grid = (unsigned)((totalTiles + 127) / 128);
+        probeTiles<<<grid, 128, 0, l.stream>>>(p, totalTiles, weights, classes);
+        placeTiles<<<grid, 128, 0, l.stream>>>(p, totalTiles, weights, classes, cursors, order);
+        p.order = order;
     }
     traceMixedQueue<<<mixedGrid(l, totalUnits), block, 0, l.stream>>>(p);
     if (combinePixels > 0)

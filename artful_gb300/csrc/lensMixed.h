@@ -17,12 +17,16 @@ namespace artf {
 constexpr size_t kMixedViewBytesMax = 1152;
 
 size_t mixedViewBytes();
-/* Fills one table slot; returns the view's unit count.  rayOut: the view's ray planes (width * height
- * float4 a ray of a pixel, mixedRayPlanes of them), or NULL.  With planes a work unit is one ray, so
- * no lane is left with a pixel's several long rays after the queue empties; without, a unit is a pixel. */
+/* Fills one table slot; returns the view's unit count and, in *tiles, its 8 x 4 tiles.  rayOut: the
+ * view's ray planes (width * height float4 a ray of a pixel, mixedRayPlanes of them), or NULL.  With
+ * planes a work unit is one ray, so no lane is left with a pixel's several long rays after the queue
+ * empties; without, a unit is a pixel.  unitBase, tileBase: the view's first unit and tile in the
+ * batch. */
 int mixedFillView(const TraceLaunch& options, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
                   const float* map, const float* fluid, float4* hdr, ArtfCudaRayEnd* ends, float4* rayOut, int unitBase,
-                  void* slot);
+                  int tileBase, void* slot, int* tiles);
+/* Device bytes of the heavy-first order of a batch of this many tiles and units. */
+size_t mixedOrderBytes(int totalTiles, int totalUnits);
 /* The planes a view needs: rays a pixel when above one, else none. */
 inline size_t mixedRayPlanes(const TraceLaunch& l, const ArtfCudaHoleFrame& frame) {
     const size_t rays = l.jitter ? (size_t)l.jitter : (size_t)frame.size[2] * frame.size[2];
@@ -32,8 +36,10 @@ inline size_t mixedRayPlanes(const TraceLaunch& l, const ArtfCudaHoleFrame& fram
 int mixedGrid(const TraceLaunch& options, int totalUnits);
 /* Launches the trace of a table already on the device (or, with options.rayCount > 0, the ray list of
  * its first view); then, when combinePixels (the largest view's pixel count) is above 0, the sum of
- * the views' ray planes into their frames. */
+ * the views' ray planes into their frames.  With orderScratch (mixedOrderBytes of device memory) and
+ * options.order heavy-first, the tiles are probed and ordered first (two short launches); NULL: the
+ * queue runs in pixel order. */
 cudaError_t launchMixedTable(const TraceLaunch& options, const void* deviceTable, int viewCount, int totalUnits,
-                             size_t combinePixels);
+                             size_t combinePixels, int totalTiles, void* orderScratch);
 
 }  // namespace artf

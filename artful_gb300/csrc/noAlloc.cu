@@ -103,19 +103,22 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     /* the table, built on this thread's stack and copied in (a copy from pageable memory is staged
      * before the call returns, so the stack buffer may go) */
     alignas(16) unsigned char stage[ARTF_CUDA_NOALLOC_MAX_VIEWS * artf::kMixedViewBytesMax];
-    long long units = 0;
+    long long units = 0, tiles = 0;
     for (int i = 0; i < count; ++i) {
-        /* (no ray planes: the fixed scratch cannot hold them, so a work unit is a pixel) */
+        /* (no ray planes nor heavy-first order: the fixed scratch cannot hold them, so a work unit is a
+         * pixel, in pixel order) */
+        int viewTiles = 0;
         units += artf::mixedFillView(l, views[i].frame, views[i].frame64, views[i].map, views[i].fluid,
-                                     (float4*)views[i].hdr, views[i].ends, nullptr, (int)units,
-                                     stage + artf::mixedViewBytes() * (size_t)i);
+                                     (float4*)views[i].hdr, views[i].ends, nullptr, (int)units, (int)tiles,
+                                     stage + artf::mixedViewBytes() * (size_t)i, &viewTiles);
+        tiles += viewTiles;
         if (units > 0x7FFFFFFFLL) return artf::failWith(ARTF_CUDA_EINVAL, "batch is too large");
     }
     unsigned char* table = scratch + kCounterBytes;
     cudaError_t e = cudaMemcpyAsync(table, stage, artf::mixedViewBytes() * (size_t)count, cudaMemcpyHostToDevice,
                                     l.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kCounterBytes, l.stream);
-    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0);
+    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0, (int)tiles, nullptr);
     if (e != cudaSuccess) {
         snprintf(line, sizeof line, "allocation-free batch launch: %s", cudaGetErrorString(e));
         return artf::failWith(ARTF_CUDA_ELAUNCH, line);

@@ -199,7 +199,13 @@ typedef struct ArtfCudaTraceOptions {
                           * (vulkan.c:1729-1756).  0: the reference's choice, bands of 8e6 rays for frames
                           * above 6.4e7 (a 4K frame of 64 rays a pixel is seconds of work); < 0: never.
                           * Single frames only; the result is the same bits either way */
+    int order;           /* mixed: the order the queue hands out work.  0: heavy first (one probe ray a tile
+                          * estimates each 8 x 4 tile's steps, and the heaviest go first, so that the
+                          * launch does not end on long rays started late); 1: pixel order.  The result is
+                          * the same bits either way */
 } ArtfCudaTraceOptions;
+
+enum { ARTF_CUDA_ORDER_HEAVY_FIRST = 0, ARTF_CUDA_ORDER_PIXELS = 1 };
 
 /* The mixed trace's FP64 guards. */
 enum {

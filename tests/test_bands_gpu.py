@@ -78,3 +78,23 @@ def test_bands_of_an_odd_frame(lib, ctx, c2):
     banded, _, s2 = _trace(lib, ctx, torch, frame, frame64, capi.MIXED, 4, 101 * 4 * 4)
     assert s2.bands == 17
     np.testing.assert_array_equal(whole.view(np.uint32), banded.view(np.uint32))
+
+
+def test_heavy_first_frames_are_the_same_bits(lib, ctx, c2):
+    """1080p, 4 rays a pixel, mixed: heavy tiles first (the default) against pixel order, whole and in
+    bands: the frame and every ray's end the same bytes."""
+    import torch
+    frame, frame64, _ = scenes.frame(c2)
+    w, h = frame.size[0], frame.size[1]
+    got = []
+    for order, band in ((capi.ORDER_PIXELS, -1), (capi.ORDER_HEAVY_FIRST, -1), (capi.ORDER_HEAVY_FIRST, 2_000_000)):
+        hdr = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+        e = torch.empty((w * h * 4 * 32,), dtype=torch.uint8, device="cuda")
+        opts = capi.TraceOptions(capi.MIXED, 4, 1, 1.0, 0.0, 0, 0, 1, 0, 0, 0, band, order)
+        stats = capi.TraceStats()  # (given: the call waits for its stream)
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts),
+                                         hdr.data_ptr(), e.data_ptr(), C.byref(stats)))
+        got.append((hdr.cpu().numpy().view(np.uint32), e.cpu().numpy()))
+    for hdr, e in got[1:]:
+        np.testing.assert_array_equal(hdr, got[0][0])
+        np.testing.assert_array_equal(e, got[0][1])

@@ -11,8 +11,9 @@ from tests import gpu_helpers as g
 pytestmark = pytest.mark.gpu
 
 
-def _views(lib, count=6, scale=0.25):
-    """Views of configuration 3 (seed 2), shrunk so the test stays small, each with its own map."""
+def _views(lib, count=6, scale=0.25, rays=1):
+    """Views of configuration 3 (seed 2), shrunk so the test stays small, each with its own map, and room
+    for the ends of `rays` rays a pixel (the views' own 1 x 1 samples, or a jitter of that many)."""
     import torch
     out, keep = [], []
     for scene in scenes.config3_views(count, seed=2):
@@ -22,7 +23,8 @@ def _views(lib, count=6, scale=0.25):
         m = torch.from_numpy(scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)).cuda()
         fluid = torch.from_numpy(scenes.unit_fluid()).cuda()
         hdr = torch.zeros((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
-        ends = torch.zeros((scene.width * scene.height * 32,), dtype=torch.uint8, device="cuda")
+        assert scene.desc.samples == 1
+        ends = torch.zeros((scene.width * scene.height * rays * 32,), dtype=torch.uint8, device="cuda")
         out.append(capi.View(frame, frame64, m.data_ptr(), fluid.data_ptr(), hdr.data_ptr(), ends.data_ptr()))
         keep.append((scene, m, fluid, hdr, ends))
     return (capi.View * len(out))(*out), keep
@@ -139,3 +141,29 @@ def test_device_loss_injected_on_the_host(lib):
                                              hdr.data_ptr(), None, None) == 0
         finally:
             lib.artfCudaDestroy(handle)
+
+
+@pytest.mark.parametrize("jitter", [0, 3])
+def test_heavy_first_gives_the_same_bits(lib, ctx, jitter):
+    """The queue's order (ArtfCudaTraceOptions.order) changes when a ray is traced, never what it computes:
+    a batch of uneven views, one ray a pixel (a unit a pixel) and three (a unit a ray), heavy tiles first
+    against pixel order, frames and ray ends the same bytes, and the same counts."""
+    import torch
+    views, keep = _views(lib, rays=max(jitter, 1))
+    out = {}
+    for order in (capi.ORDER_HEAVY_FIRST, capi.ORDER_PIXELS):
+        stats = capi.TraceStats()
+        for *_, hdr, ends in keep:
+            hdr.zero_()
+            ends.zero_()
+        capi.check(lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts(jitter=jitter, order=order)),
+                                         C.byref(stats)))
+        torch.cuda.synchronize()
+        out[order] = ([(hdr.cpu().numpy().copy(), ends.cpu().numpy().copy()) for *_, hdr, ends in keep],
+                      (stats.rays, stats.steps, stats.crossings, stats.escapes, stats.fp64Steps))
+    (a, sa), (b, sb) = out[capi.ORDER_HEAVY_FIRST], out[capi.ORDER_PIXELS]
+    assert sa == sb
+    for i, ((ha, ea), (hb, eb)) in enumerate(zip(a, b)):
+        assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32)), i
+        assert np.array_equal(ea, eb), i
+    assert lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts(order=2)), None) == -1  # ARTF_CUDA_EINVAL
