@@ -253,13 +253,28 @@ template <typename R> ARTF_HD R bendAt(const RayConst<R>& c, R x) { return x * (
  * So one Nystrom step is a radial sub-step of (u, w, psi) and a polar sub-step of (n, v), with the same
  * operations either way; the mixed-precision trace runs each in the precision it needs. */
 
-/* lens.inc:165-192, the radial part: u, du/ds, and Simpson's rule for psi. */
+/* The products of a ray's step that every sub-step takes (lens.inc:165-192): fixed along the ray, so a
+ * caller may form them once and hand them to the sub-steps below, with the same values. */
+template <typename R> struct StepTerms {
+    R half, eighth, halfSquare, sixthSquare, sixth;
+};
+
+template <typename R> ARTF_HD StepTerms<R> stepTerms(R step) {
+    const R step2 = step * step;
+    StepTerms<R> t;
+    t.half = step * KF(.5), t.eighth = step2 * KF(.125), t.halfSquare = step2 * KF(.5);
+    t.sixthSquare = step2 * R(1.f / 6.f), t.sixth = step * R(1.f / 6.f);
+    return t;
+}
+
+/* lens.inc:165-192, the radial part: u, du/ds, and Simpson's rule for psi, with the step's terms and
+ * a2 = a * a given. */
 template <typename R>
-ARTF_HD void radialStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R& k1Out) {
-    const R a2 = a * a;
-    const R step = c.step, step2 = step * step;
-    const R half = step * KF(.5), eighth = step2 * KF(.125), halfSquare = step2 * KF(.5);
-    const R sixthSquare = step2 * R(1.f / 6.f), sixth = step * R(1.f / 6.f);
+ARTF_HD void radialStepWith(R a, R a2, const RayConst<R>& c, const StepTerms<R>& t, const RayState<R>& s,
+                            RayState<R>& next, R& k1Out) {
+    const R step = c.step;
+    const R half = t.half, eighth = t.eighth, halfSquare = t.halfSquare;
+    const R sixthSquare = t.sixthSquare, sixth = t.sixth;
     const R k1 = bendAt(c, s.u);
     const R midU = s.u + half * s.w + eighth * k1;
     const R k2 = bendAt(c, midU);
@@ -277,13 +292,19 @@ ARTF_HD void radialStep(R a, const RayConst<R>& c, const RayState<R>& s, RayStat
     k1Out = k1;
 }
 
-/* lens.inc:165-192, the polar part: n on the sphere and dn/ds. */
 template <typename R>
-ARTF_HD void polarStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R* a1Out) {
-    const R a2 = a * a, twoA2 = KF(2.) * a2;
-    const R step = c.step, step2 = step * step;
-    const R half = step * KF(.5), eighth = step2 * KF(.125), halfSquare = step2 * KF(.5);
-    const R sixthSquare = step2 * R(1.f / 6.f), sixth = step * R(1.f / 6.f);
+ARTF_HD void radialStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R& k1Out) {
+    radialStepWith(a, a * a, c, stepTerms(c.step), s, next, k1Out);
+}
+
+/* lens.inc:165-192, the polar part: n on the sphere and dn/ds, with the step's terms, a2 = a * a and
+ * twoA2 = 2 * a2 given. */
+template <typename R>
+ARTF_HD void polarStepWith(R a2, R twoA2, const RayConst<R>& c, const StepTerms<R>& t, const RayState<R>& s,
+                           RayState<R>& next, R* a1Out) {
+    const R step = c.step;
+    const R half = t.half, eighth = t.eighth, halfSquare = t.halfSquare;
+    const R sixthSquare = t.sixthSquare, sixth = t.sixth;
     const R c1 = c.big + twoA2 * (s.n[2] * s.n[2]);
     const R a1[3] = {R(0) - c1 * s.n[0], R(0) - c1 * s.n[1], a2 * s.n[2] - c1 * s.n[2]};
     R midN[3];
@@ -299,6 +320,12 @@ ARTF_HD void polarStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState
         next.v[k] = s.v[k] + sixth * (a1[k] + a3[k] + KF(4.) * a2s[k]);
         a1Out[k] = a1[k];
     }
+}
+
+template <typename R>
+ARTF_HD void polarStep(R a, const RayConst<R>& c, const RayState<R>& s, RayState<R>& next, R* a1Out) {
+    const R a2 = a * a;
+    polarStepWith(a2, KF(2.) * a2, c, stepTerms(c.step), s, next, a1Out);
 }
 
 /* lens.inc:165-192: one Nystrom step of (u, n) and Simpson's rule for psi. */

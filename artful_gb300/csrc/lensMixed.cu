@@ -46,6 +46,7 @@ struct MixedView {
      * unit is one ray and mixedCombine sums each pixel's rays afterwards; without, a unit is a pixel
      * whose rays one lane traces in turn. */
     float4* rayOut;
+    double wideA2, wideTwoA2; /* a^2 and 2 a^2 in double, for the FP64 sub-steps */
     float rhoScale, uGuard, share;
     int tilesX, pixelUnits, units, unitBase, tileBase, rays, jitter;
     int rowBegin, rows; /* the pixel rows this launch traces (a band of the frame, or all of it) */
@@ -128,20 +129,23 @@ __device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedView
     reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
 }
 
-__device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, StepOut<float>& o) {
+/* The FP64 sub-steps, with the ray's step terms (stepTerms(r.step), formed once a ray). */
+__device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
+                                           StepOut<float>& o) {
     RayState<double> s, next;
     s.u = r.s.u, s.w = r.s.w, s.psi = 0.0, s.drag = r.s.drag;
     double k1;
-    radialStep(v.d.a, wideConst(r), s, next, k1);
+    radialStepWith(v.d.a, v.wideA2, wideConst(r), t, s, next, k1);
     o.next.u = (float)next.u, o.next.w = (float)next.w, o.next.psi = (float)next.psi, o.next.drag = (float)next.drag;
     o.k1 = (float)k1;
 }
 
-__device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, StepOut<float>& o) {
+__device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
+                                          StepOut<float>& o) {
     RayState<double> s, next;
     for (int k = 0; k < 3; ++k) s.n[k] = r.s.n[k], s.v[k] = r.s.v[k];
     double a1[3];
-    polarStep(v.d.a, wideConst(r), s, next, a1);
+    polarStepWith(v.wideA2, v.wideTwoA2, wideConst(r), t, s, next, a1);
     for (int k = 0; k < 3; ++k) o.next.n[k] = (float)next.n[k], o.next.v[k] = (float)next.v[k], o.a1[k] = (float)a1[k];
 }
 
@@ -239,8 +243,11 @@ __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const Mi
         bool radial, polar;
         unsigned reason;
         mixedNeeds(p, v, r, o, radial, polar, reason);
-        if (radial) radialWide(v, r, o);
-        if (polar) polarWide(v, r, o);
+        if (radial || polar) {
+            const StepTerms<double> terms = stepTerms(r.step);
+            if (radial) radialWide(v, r, terms, o);
+            if (polar) polarWide(v, r, terms, o);
+        }
         if (radial || polar) {
             ++r.wide;
             countReason(reason, n);
@@ -343,8 +350,19 @@ __global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int total
     for (unsigned k = 0; k < planes; ++k) order[at + k] = make_uint2((unsigned)vi | k << 12, (unsigned)(g - v.tileBase));
 }
 
+/* This lane's step terms, from the block's table. */
+__device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256]) {
+    StepTerms<double> t;
+    t.half = terms[0][threadIdx.x], t.eighth = terms[1][threadIdx.x], t.halfSquare = terms[2][threadIdx.x];
+    t.sixthSquare = terms[3][threadIdx.x], t.sixth = terms[4][threadIdx.x];
+    return t;
+}
+
 /* The warp-scheduled trace (see the file's head). */
 __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
+    /* each lane's ray's step terms in double, formed at its set-up: an FP64 round then loads them
+     * where it would multiply them out again (FP64 multiplies are the scarce resource) */
+    __shared__ double terms[5][256];
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -409,6 +427,10 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                 float nx, ny, moment;
                 samplePosition(v->h, v->jitter, v->seed, x, y, k, &nx, &ny, &moment);
                 mixedStart(p, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
+                const StepTerms<double> t = stepTerms(r.step);
+                terms[0][threadIdx.x] = t.half, terms[1][threadIdx.x] = t.eighth;
+                terms[2][threadIdx.x] = t.halfSquare, terms[3][threadIdx.x] = t.sixthSquare;
+                terms[4][threadIdx.x] = t.sixth;
                 live = true;
             }
         } else if (idle) {
@@ -431,7 +453,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
         if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
             if (waitR) {
-                radialWide(*v, r, o);
+                radialWide(*v, r, laneTerms(terms), o);
                 waitR = false;
             }
             sinceRadial = 0;
@@ -441,7 +463,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         }
         if (needP && (__popc(needP) >= p.batch || ready == 0 || sincePolar >= p.maxWait)) {
             if (waitP) {
-                polarWide(*v, r, o);
+                polarWide(*v, r, laneTerms(terms), o);
                 waitP = false;
             }
             sincePolar = 0;
@@ -545,6 +567,8 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.fluid = fluid;
     v.hdr = hdr;
     v.ends = ends;
+    v.wideA2 = v.d.a * v.d.a;
+    v.wideTwoA2 = 2.0 * v.wideA2;
     v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
     v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * frame64.spin[1]);
     v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);
