@@ -198,9 +198,26 @@ template <typename R> struct StepOut {
     R k1, a1[3];
 };
 
+/* What a ray's start takes from the frame alone (lens.inc:125-152), fixed for a view and a step scale:
+ * a caller may form it once and hand it to rayStartWith, with the same values. */
+template <typename R> struct StartTerms {
+    R a2, mu0Squared, minusTwoA2, stepBase, wScale;
+};
+
+template <typename R> ARTF_HD StartTerms<R> startTerms(const Frame<R>& f, R stepScale) {
+    const R u0 = f.place[2];
+    StartTerms<R> t;
+    t.a2 = f.a * f.a;
+    t.mu0Squared = f.place[3] * f.place[3];
+    t.minusTwoA2 = KF(-2.) * t.a2;
+    t.stepBase = KF(.13089969) * stepScale;
+    t.wScale = (-u0) * u0 * f.place[1] * f.place[0];
+    return t;
+}
+
 /* lens.inc:101-152: the ray of image position (nx, ny), its constants of motion, its first state. */
-template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R time, R stepScale, RayConst<R>& c,
-                                            RayState<R>& s) {
+template <typename R> ARTF_HD void rayStartWith(const Frame<R>& f, const StartTerms<R>& t, R nx, R ny, R time,
+                                                RayConst<R>& c, RayState<R>& s) {
     R d[3];
     for (int k = 0; k < 3; ++k) d[k] = f.forward[k] + nx * f.right[k] + ny * f.up[k];
     const R invLength = invSqrtR(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -218,28 +235,33 @@ template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R tim
         moved = over;
     }
 
-    const R a = f.a, a2 = a * a, rho = f.place[0], rootDelta = f.place[1], u0 = f.place[2], mu0 = f.place[3];
+    const R a = f.a, a2 = t.a2, rho = f.place[0], u0 = f.place[2];
     const R energy = f.metric[0] - f.metric[1] * d[2];
     c.invEnergy = recipR(energy);
     c.xi = R(0) - f.metric[2] * d[2] * c.invEnergy;
     const R xiAxis = f.metric[3] * d[2] * c.invEnergy;
     const R across = rho * d[1] * c.invEnergy;
-    const R eta = across * across + mu0 * mu0 * (xiAxis * xiAxis - a2);
+    const R eta = across * across + t.mu0Squared * (xiAxis * xiAxis - a2);
     c.big = eta + c.xi * c.xi;
-    c.step = divSqrtR(KF(.13089969) * stepScale, maxX(c.big, KF(4.)));
+    c.step = divSqrtR(t.stepBase, maxX(c.big, KF(4.)));
     c.uA = a2 - c.big;
     const R xiOff = c.xi - a;
     c.uB = KF(3.) * (eta + xiOff * xiOff);
-    c.uC = (KF(-2.) * a2) * eta;
+    c.uC = t.minusTwoA2 * eta;
     c.xiA = c.xi * a;
     c.moved = moved;
     c.time = time;
 
     s.u = u0;
-    s.w = ((-u0) * u0 * rootDelta * rho) * d[0] * c.invEnergy;
+    s.w = t.wScale * d[0] * c.invEnergy;
     for (int k = 0; k < 3; ++k) s.n[k] = f.er[k], s.v[k] = across * f.etheta[k] + xiAxis * f.ephi[k];
     s.psi = R(0);
     s.drag = R(0);
+}
+
+template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R time, R stepScale, RayConst<R>& c,
+                                            RayState<R>& s) {
+    rayStartWith(f, startTerms(f, stepScale), nx, ny, time, c, s);
 }
 
 /* psi' at u (lens.inc:144 DRAG); the denominator is Delta / r^2, kept off zero. */

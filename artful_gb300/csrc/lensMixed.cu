@@ -47,6 +47,8 @@ struct MixedView {
      * whose rays one lane traces in turn. */
     float4* rayOut;
     double wideA2, wideTwoA2; /* a^2 and 2 a^2 in double, for the FP64 sub-steps */
+    StartTerms<double> start64; /* what each ray's FP64 set-up takes from the view alone */
+    float startNarrow[4];     /* the eye's e_r and 1/r in float, where every ray's FP64 set-up starts */
     float rhoScale, uGuard, share;
     int tilesX, pixelUnits, units, unitBase, tileBase, rays, jitter;
     int rowBegin, rows; /* the pixel rows this launch traces (a band of the frame, or all of it) */
@@ -96,13 +98,15 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, const MixedView
     if (p.guards & ARTF_CUDA_GUARD_MOTION) {
         RayConst<double> cd;
         RayState<double> sd;
-        rayStart(v.d, (double)nx, (double)ny, (double)time, (double)p.stepScale, cd, sd);
-        r.c.invEnergy = (float)cd.invEnergy, r.c.xi = (float)cd.xi, r.c.moved = (float)cd.moved;
+        rayStartWith(v.d, v.start64, (double)nx, (double)ny, (double)time, cd, sd);
+        r.c.invEnergy = (float)cd.invEnergy, r.c.xi = (float)cd.xi;
+        r.c.moved = v.d.boost[3] > 1.0 ? (float)cd.moved : 1.f; /* (1 for an eye at rest) */
         r.c.big = (float)cd.big, r.c.step = (float)cd.step, r.c.uA = (float)cd.uA, r.c.uB = (float)cd.uB;
         r.c.uC = (float)cd.uC, r.c.xiA = (float)cd.xiA;
         r.big = cd.big, r.step = cd.step, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
-        r.s.u = (float)sd.u, r.s.w = (float)sd.w;
-        for (int k = 0; k < 3; ++k) r.s.n[k] = (float)sd.n[k], r.s.v[k] = (float)sd.v[k];
+        /* (u and n start at the eye's: the view's, narrowed once) */
+        r.s.u = v.startNarrow[3], r.s.w = (float)sd.w;
+        for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = (float)sd.v[k];
     } else {
         rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
         r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
@@ -569,6 +573,9 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.ends = ends;
     v.wideA2 = v.d.a * v.d.a;
     v.wideTwoA2 = 2.0 * v.wideA2;
+    v.start64 = startTerms(v.d, (double)l.stepScale);
+    for (int k = 0; k < 3; ++k) v.startNarrow[k] = (float)v.d.er[k];
+    v.startNarrow[3] = (float)v.d.place[2];
     v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
     v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * frame64.spin[1]);
     v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);
