@@ -86,7 +86,7 @@ class TraceStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("steps", C.c_uint64), ("crossings", C.c_uint64), ("escapes", C.c_uint64),
                 ("fp64Steps", C.c_uint64), ("fp64Horizon", C.c_uint64), ("fp64Radial", C.c_uint64),
                 ("fp64Polar", C.c_uint64), ("fp64Rounds", C.c_uint64), ("flops", C.c_double), ("ms", C.c_float),
-                ("bands", C.c_uint32)]
+                ("bands", C.c_uint32), ("flops64", C.c_double)]
 
 
 class View(C.Structure):

@@ -363,7 +363,8 @@ static int waitStaging(ArtfCuda* ctx) {
     return ARTF_CUDA_OK;
 }
 
-static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precision, ArtfCudaTraceStats* stats) {
+static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precision, uint32_t guards,
+                     ArtfCudaTraceStats* stats) {
     unsigned long long c[artf::CCount];
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(c, ctx->counters, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
@@ -380,6 +381,15 @@ static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precisio
     stats->fp64Rounds = c[artf::CFp64Rounds];
     stats->flops = artfFlops(stats->rays, stats->steps, stats->crossings, stats->escapes, frame.spin[0] != 0.f,
                              frame.look[1] != 0.f, frame.look[2] > 0.f);
+    if (precision == ARTF_CUDA_FP64) {
+        stats->flops64 = stats->flops;
+    } else if (precision == ARTF_CUDA_MIXED) {
+        const bool motion = (guards ? guards : ARTF_CUDA_GUARD_ALL) & ARTF_CUDA_GUARD_MOTION;
+        stats->flops64 = artfFlops64(motion ? stats->rays : 0, stats->fp64Horizon + stats->fp64Radial,
+                                     stats->fp64Polar, frame.spin[0] != 0.f);
+    } else {
+        stats->flops64 = 0.0;
+    }
     stats->ms = ms;
     stats->bands = ctx->lastBands;
     return ARTF_CUDA_OK;
@@ -455,7 +465,7 @@ static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, int64_t 
     if (status) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = (uint32_t)bands;
-    return stats ? readStats(ctx, l.frame, precision, stats) : ARTF_CUDA_OK;
+    return stats ? readStats(ctx, l.frame, precision, l.guards, stats) : ARTF_CUDA_OK;
 }
 
 extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
@@ -572,7 +582,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
         return fail(status, "bloom and tone map launch: %s", cudaGetErrorString(cudaGetLastError()));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     if (stats) {
-        if ((status = readStats(ctx, *frame, options->precision, stats))) return status;
+        if ((status = readStats(ctx, *frame, options->precision, options->guards, stats))) return status;
     }
     if (hostHdr)
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostHdr, ctx->hdr, sizeof(float4) * pixels,
@@ -758,7 +768,7 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
-    return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
+    return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, l.guards, stats) : ARTF_CUDA_OK;
 }
 
 struct ArtfCudaGraph {
@@ -868,7 +878,7 @@ extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* st
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaGraphLaunch(g->exec, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
-    return stats ? readStats(ctx, g->first, ARTF_CUDA_MIXED, stats) : ARTF_CUDA_OK;
+    return stats ? readStats(ctx, g->first, ARTF_CUDA_MIXED, g->options.guards, stats) : ARTF_CUDA_OK;
 }
 
 /* ---- the autotuner ------------------------------------------------------------------------------ */

@@ -29,6 +29,23 @@
 #define ARTF_FLOPS_ESCAPE 59
 #define ARTF_FLOPS_SKY 58
 
+/* The mixed trace's FP64 work, by the same rule, for the FP64 pipe's roofline:
+ *   per set-up   a ray's constants of motion and first state (what it takes from its view formed once a
+ *                view), and its step's terms (formed once a ray)
+ *   per radial   one radial sub-step (u, du/ds and psi) with those terms given; spin 0: no drag, no psi
+ *   per polar    one polar sub-step (n, dn/ds) */
+#define ARTF_FLOPS_WIDE_START 66
+#define ARTF_FLOPS_WIDE_RADIAL 61
+#define ARTF_FLOPS_WIDE_RADIAL_SPINLESS 34
+#define ARTF_FLOPS_WIDE_POLAR 87
+
+static inline double artfFlops64(unsigned long long setups, unsigned long long radial, unsigned long long polar,
+                                 int spinning) {
+    return ARTF_FLOPS_WIDE_START * (double)setups +
+           (spinning ? ARTF_FLOPS_WIDE_RADIAL : ARTF_FLOPS_WIDE_RADIAL_SPINLESS) * (double)radial +
+           ARTF_FLOPS_WIDE_POLAR * (double)polar;
+}
+
 static inline double artfFlops(unsigned long long rays, unsigned long long steps, unsigned long long crossings,
                                unsigned long long escapes, int spinning, int doppler, int stars) {
     const double perRay = spinning ? ARTF_FLOPS_RAY : ARTF_FLOPS_RAY_SPINLESS;

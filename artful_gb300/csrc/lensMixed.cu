@@ -293,10 +293,12 @@ __device__ __forceinline__ int viewOf(const MixedParams& p, int unit) {
  * while the others idle (a photon-ring ray runs to the step cap, ten times a sky ray's steps).  So the
  * queue hands out the heaviest tiles first and leaves short rays for the end.  A tile's weight is the
  * step count of one FP32 ray through its middle, stepped without shading (the disc is thin: it seldom
- * ends a ray); tiles are counting-sorted by weight class, heaviest first.  The order changes when a ray
- * is traced, never what it computes, so the frame is the same bits in any order. */
+ * ends a ray) up to 64 steps (a sky ray takes about 25; what goes on longer is heavy); tiles are
+ * counting-sorted by weight class, heaviest first.  The order changes when a ray is traced, never what
+ * it computes, so the frame is the same bits in any order. */
 
-constexpr int kWeightClasses = 25; /* steps / 16: the 384-step cap is class 24 */
+constexpr int kWeightClasses = 9; /* steps / 8 up to 64: the probe stops there (all heavier tiles, class 8) */
+constexpr int kProbeSteps = 64;
 
 /* The view a batch-wide tile belongs to: the last whose first tile is at or below it. */
 __device__ __forceinline__ int tileView(const MixedParams& p, int tile) {
@@ -309,49 +311,72 @@ __device__ __forceinline__ int tileView(const MixedParams& p, int tile) {
     return lo;
 }
 
-/* Each tile's weight class, and each class's count of queue slots (a tile has one a ray plane). */
+/* Each tile's weight class, and each class's count of queue slots (a tile has one a ray plane), counted
+ * in the block first so that each class takes one global atomic a block. */
 __global__ void __launch_bounds__(128) probeTiles(const MixedParams p, int totalTiles, int* weights,
                                                   unsigned* classes) {
+    __shared__ unsigned counts[kWeightClasses];
+    if (threadIdx.x < kWeightClasses) counts[threadIdx.x] = 0;
+    __syncthreads();
     const int g = (int)(blockIdx.x * 128 + threadIdx.x);
-    if (g >= totalTiles) return;
-    const MixedView& v = p.views[tileView(p, g)];
-    const int tile = g - v.tileBase;
-    const int x = min((tile % v.tilesX) * 8 + 4, (int)v.f.width - 1);
-    const int y = min(v.rowBegin + (tile / v.tilesX) * 4 + 2, v.rowBegin + v.rows - 1);
-    float nx, ny, moment;
-    samplePosition(v.h, v.jitter, v.seed, x, y, 0, &nx, &ny, &moment);
-    RayConst<float> c;
-    RayState<float> s;
-    rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, p.stepScale, c, s);
-    const float a = v.f.a;
-    if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
-    int i = 0;
-    while (i < p.maxSteps) {
-        StepOut<float> o;
-        nystromStep(a, c, s, o);
-        ++i;
-        if (0.f > o.next.u || o.next.u > v.f.uHorizon) break;
-        s = o.next;
+    if (g < totalTiles) {
+        const MixedView& v = p.views[tileView(p, g)];
+        const int tile = g - v.tileBase;
+        const int x = min((tile % v.tilesX) * 8 + 4, (int)v.f.width - 1);
+        const int y = min(v.rowBegin + (tile / v.tilesX) * 4 + 2, v.rowBegin + v.rows - 1);
+        float nx, ny, moment;
+        samplePosition(v.h, v.jitter, v.seed, x, y, 0, &nx, &ny, &moment);
+        RayConst<float> c;
+        RayState<float> s;
+        rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, p.stepScale, c, s);
+        const float a = v.f.a;
+        if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
+        const int most = min(p.maxSteps, kProbeSteps);
+        int i = 0;
+        while (i < most) {
+            StepOut<float> o;
+            nystromStep(a, c, s, o);
+            ++i;
+            if (0.f > o.next.u || o.next.u > v.f.uHorizon) break;
+            s = o.next;
+        }
+        const int w = min(i >> 3, kWeightClasses - 1);
+        weights[g] = w;
+        atomicAdd(counts + w, v.rayOut ? (unsigned)v.rays : 1u);
     }
-    const int w = min(i >> 4, kWeightClasses - 1);
-    weights[g] = w;
-    atomicAdd(classes + w, v.rayOut ? (unsigned)v.rays : 1u);
+    __syncthreads();
+    if (threadIdx.x < kWeightClasses && counts[threadIdx.x]) atomicAdd(classes + threadIdx.x, counts[threadIdx.x]);
 }
 
 /* Each tile's slots into the order, its planes together, heavier classes first (within a class in the
- * order the atomics give). */
+ * order the atomics give): a block reserves each class's run with one global atomic, its tiles take
+ * places within the run by shared ones. */
 __global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int totalTiles, const int* weights,
                                                   const unsigned* classes, unsigned* cursors, uint2* order) {
+    __shared__ unsigned counts[kWeightClasses], runs[kWeightClasses];
+    if (threadIdx.x < kWeightClasses) counts[threadIdx.x] = 0;
+    __syncthreads();
     const int g = (int)(blockIdx.x * 128 + threadIdx.x);
-    if (g >= totalTiles) return;
-    const int vi = tileView(p, g);
-    const MixedView& v = p.views[vi];
-    const int w = weights[g];
-    unsigned at = 0;
-    for (int c = kWeightClasses - 1; c > w; --c) at += classes[c];
-    const unsigned planes = v.rayOut ? (unsigned)v.rays : 1u;
-    at += atomicAdd(cursors + w, planes);
-    for (unsigned k = 0; k < planes; ++k) order[at + k] = make_uint2((unsigned)vi | k << 12, (unsigned)(g - v.tileBase));
+    const bool active = g < totalTiles;
+    int vi = 0, w = 0;
+    unsigned planes = 0, within = 0;
+    if (active) {
+        vi = tileView(p, g);
+        w = weights[g];
+        planes = p.views[vi].rayOut ? (unsigned)p.views[vi].rays : 1u;
+        within = atomicAdd(counts + w, planes);
+    }
+    __syncthreads();
+    if (threadIdx.x < kWeightClasses) {
+        unsigned before = 0;
+        for (int c = kWeightClasses - 1; c > (int)threadIdx.x; --c) before += classes[c];
+        runs[threadIdx.x] = counts[threadIdx.x] ? before + atomicAdd(cursors + threadIdx.x, counts[threadIdx.x]) : 0u;
+    }
+    __syncthreads();
+    if (!active) return;
+    const unsigned at = runs[w] + within;
+    const unsigned tile = (unsigned)(g - p.views[vi].tileBase);
+    for (unsigned k = 0; k < planes; ++k) order[at + k] = make_uint2((unsigned)vi | k << 12, tile);
 }
 
 /* This lane's step terms, from the block's table. */

@@ -37,6 +37,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "geodesics/s @1080p: mixed-prec vs FP64 GPU at ≤1e-4 endpoint err; adj/fwd time"
 UNIT = "geodesics/s"
+# Kernels one mixed frame launches: the tile probe, the heavy-first order, the trace, the ray-plane sum.
+LAUNCHES_PER_MIXED_FRAME = 4
+# DRAM bytes (read + write) of one launch of the mixed trace kernel at this workload, from one ncu
+# capture (dram__bytes_read.sum 16.46 MB + dram__bytes_write.sum 73.44 MB): the map read once, and the
+# part of the 133 MB of ray planes that leaves L2 before the sum reads it back.
+TRACE_TRAFFIC_BYTES = 89_900_000
 
 
 def parse():
@@ -395,11 +401,14 @@ def main():
             e_ref, img_ref = ends_of(capi.FP64, scale)
             endpoint[label] = endpoint_error(e_mixed, e_ref, img_mixed, img_ref)
 
-    # roofline of the trace: the FP32 pipe (the dominant kernel is FP32-bound; no tensor cores)
+    # roofline of the trace: the mixed kernel is bound by the FP64 pipe (its FP64 set-ups and sub-steps:
+    # the pipe is 1/72 of the FP32 one); no tensor cores.  Both pipes' algorithmic work over the step time
     fp32_peak, fp64_peak = C.c_double(), C.c_double()
     capi.check(lib.artfCudaProbePeaks(lib.artfCudaStream(ctx), local, C.byref(fp32_peak), C.byref(fp64_peak)))
     achieved = s_mixed.flops / (ms_mixed * 1e-3) / 1e12
     peak = fp32_peak.value / 1e12
+    achieved64 = s_mixed.flops64 / (ms_mixed * 1e-3) / 1e12
+    peak64 = fp64_peak.value / 1e12
 
     # end to end through the host-buffer entry point
     pin_map = torch.from_numpy(map_).pin_memory()
@@ -442,15 +451,17 @@ def main():
         "fp64_step_share": s_mixed.fp64Steps / max(1, s_mixed.steps),
         "side": side,
         "endpoint_error": endpoint,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_source": "measured FMA-chain probe (artfCudaProbePeaks); MEASURED_PEAKS.json has no "
-                                    "FP32-pipe figure",
-                     "fp64_peak_tflops": fp64_peak.value / 1e12,
-                     "flops_per_frame": s_mixed.flops},
+        "roofline": {"bound": "fp64", "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": achieved64 / peak64, "traffic": TRACE_TRAFFIC_BYTES,
+                     "peak_source": "measured FMA-chain probe (artfCudaProbePeaks), of measured; "
+                                    "MEASURED_PEAKS.json has no FP64- or FP32-pipe figure",
+                     "flops64_per_frame": s_mixed.flops64,
+                     "fp32": {"achieved": achieved, "peak": peak, "frac": achieved / peak,
+                              "flops_per_frame": s_mixed.flops},
+                     "time": "the whole timed step (probe, order, trace, combine)"},
         "e2e": {"value": world * geodesics / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": (map_.nbytes + fluid.nbytes), "d2h_bytes_per_step": h * w * 16},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * LAUNCHES_PER_MIXED_FRAME,
         "clocks": clocks.summary(),
     }
     if cpu:

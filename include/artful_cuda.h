@@ -248,6 +248,8 @@ typedef struct ArtfCudaTraceStats {
     double flops;        /* algorithmic FP32-pipe operations (the counting rule is in lensFlops.h) */
     float ms;            /* device time of the trace kernel(s), CUDA events on the context's stream */
     uint32_t bands;      /* launches the frame went out in (ArtfCudaTraceOptions.bandRays) */
+    double flops64;      /* of the work, what ran on the FP64 pipe (FP64: all of flops; mixed: the FP64
+                          * set-ups and sub-steps, by the same rule) */
 } ArtfCudaTraceStats;
 
 /* Traces one frame into `hdr` (device memory, width * height float4: linear RGB and the class bits).

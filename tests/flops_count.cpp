@@ -83,6 +83,25 @@ int main() {
         if (f.a != Op(0.0)) s.drag = dragAt(f.a, f.a * f.a, c.xiA, s.u);
         const Op rhoScale = recipR(Op(1.0) - divR(f.inner, f.outer));
         printf("setup%s %ld\n", tag, g_ops);
+        /* the mixed trace's FP64 work: a ray's set-up (what it takes from the view formed once a view,
+         * its step's terms formed once a ray), and one radial and one polar sub-step with those given */
+        {
+            const StartTerms<Op> view = startTerms(f, Op(1.0));
+            const Op a2 = f.a * f.a, twoA2 = Op(2.0) * a2;
+            RayConst<Op> cw;
+            RayState<Op> sw, next;
+            Op k1, a1[3];
+            g_ops = 0;
+            rayStartWith(f, view, Op(0.1), Op(0.2), Op(0.0), cw, sw);
+            const StepTerms<Op> terms = stepTerms(cw.step);
+            printf("wide_start%s %ld\n", tag, g_ops);
+            g_ops = 0;
+            radialStepWith(f.a, a2, cw, terms, sw, next, k1);
+            printf("wide_radial%s %ld\n", tag, g_ops);
+            g_ops = 0;
+            polarStepWith(a2, twoA2, cw, terms, sw, next, a1);
+            printf("wide_polar%s %ld\n", tag, g_ops);
+        }
         /* one Nystrom step as written: each sub-step recomputes the ray's constant products */
         StepOut<Op> o;
         g_ops = 0;

@@ -58,3 +58,12 @@ def test_per_escape(counts, constants):
     assert constants["SKY"] == counts["sky"] == counts["sky_spinless"]
     # a star drawn in both layers' cells: the most the lower bound leaves out
     assert counts["sky_with_stars"] - counts["sky"] == 63
+
+
+def test_mixed_fp64_work(counts, constants):
+    """The mixed trace's FP64 pipe work: a ray's set-up with its view's terms given (and its step's terms
+    formed), and one radial and one polar sub-step with those terms given."""
+    assert constants["WIDE_START"] == counts["wide_start"] == counts["wide_start_spinless"]
+    assert constants["WIDE_RADIAL"] == counts["wide_radial"]
+    assert constants["WIDE_RADIAL_SPINLESS"] == counts["wide_radial_spinless"]
+    assert constants["WIDE_POLAR"] == counts["wide_polar"] == counts["wide_polar_spinless"]
