@@ -85,6 +85,42 @@ struct MixedRay {
     bool lit;
 };
 
+/* Float <-> double conversions on the integer pipe.  On this GPU a conversion to double costs an FP64
+ * instruction and one to float two, on the FP64 pipe that bounds this kernel, while the integer pipe
+ * idles: these take a handful of integer instructions instead, for the same bits as the hardware's
+ * conversions under this unit's flags (flush-to-zero; round to nearest even), NaN aside (a NaN stays a
+ * NaN, its payload is not kept).  artfCudaCheckConversions checks them against the hardware's. */
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t b = __float_as_uint(f), sign = b & 0x80000000u, mag = b & 0x7fffffffu, e = mag >> 23;
+    uint32_t hi = sign | ((mag >> 3) + 0x38000000u), lo = mag << 29;  /* rebias 127 -> 1023 */
+    if (e == 0u) hi = sign, lo = 0u;                                    /* zero (a subnormal flushes) */
+    if (e == 255u) hi = sign | 0x7ff00000u | ((mag & 0x7fffffu) >> 3);  /* infinity, NaN */
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float narrow(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t sign = hi & 0x80000000u, e = (hi >> 20) & 0x7ffu;
+    /* the top 23 bits of the 52-bit fraction, and the 29 below them that rounding looks at */
+    const uint32_t keep = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
+    uint32_t bits;
+    if (e >= 897u && e <= 1150u) {
+        bits = ((e - 896u) << 23) | keep;
+        bits += (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) ? 1u : 0u; /* (may carry to inf) */
+    } else if (e == 896u) {
+        /* in [2^-127, 2^-126): rounded to 24 significant bits as if the exponent went on, only what then
+         * reaches 2^-126 is not flushed (the fraction's top 23 bits all ones, and the rest half or more) */
+        bits = (keep == 0x7fffffu && rest >= 0x10000000u) ? 0x00800000u : 0u;
+    } else if (e < 896u) {
+        bits = 0u;
+    } else if (e == 0x7ffu && ((hi & 0xfffffu) | lo)) {
+        bits = 0x7fffffffu; /* NaN */
+    } else {
+        bits = 0x7f800000u; /* too large, or infinite */
+    }
+    return __uint_as_float(sign | bits);
+}
+
 __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
     RayConst<double> c;
     c.big = r.big, c.step = r.step, c.uA = r.uA, c.uB = r.uB, c.uC = r.uC, c.xiA = r.xiA;
@@ -98,15 +134,15 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, const MixedView
     if (p.guards & ARTF_CUDA_GUARD_MOTION) {
         RayConst<double> cd;
         RayState<double> sd;
-        rayStartWith(v.d, v.start64, (double)nx, (double)ny, (double)time, cd, sd);
-        r.c.invEnergy = (float)cd.invEnergy, r.c.xi = (float)cd.xi;
-        r.c.moved = v.d.boost[3] > 1.0 ? (float)cd.moved : 1.f; /* (1 for an eye at rest) */
-        r.c.big = (float)cd.big, r.c.step = (float)cd.step, r.c.uA = (float)cd.uA, r.c.uB = (float)cd.uB;
-        r.c.uC = (float)cd.uC, r.c.xiA = (float)cd.xiA;
+        rayStartWith(v.d, v.start64, widen(nx), widen(ny), widen(time), cd, sd);
+        r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi);
+        r.c.moved = v.d.boost[3] > 1.0 ? narrow(cd.moved) : 1.f; /* (1 for an eye at rest) */
+        r.c.big = narrow(cd.big), r.c.step = narrow(cd.step), r.c.uA = narrow(cd.uA), r.c.uB = narrow(cd.uB);
+        r.c.uC = narrow(cd.uC), r.c.xiA = narrow(cd.xiA);
         r.big = cd.big, r.step = cd.step, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
         /* (u and n start at the eye's: the view's, narrowed once) */
-        r.s.u = v.startNarrow[3], r.s.w = (float)sd.w;
-        for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = (float)sd.v[k];
+        r.s.u = v.startNarrow[3], r.s.w = narrow(sd.w);
+        for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = narrow(sd.v[k]);
     } else {
         rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
         r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
@@ -137,20 +173,20 @@ __device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedView
 __device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
                                            StepOut<float>& o) {
     RayState<double> s, next;
-    s.u = r.s.u, s.w = r.s.w, s.psi = 0.0, s.drag = r.s.drag;
+    s.u = widen(r.s.u), s.w = widen(r.s.w), s.psi = 0.0, s.drag = widen(r.s.drag);
     double k1;
     radialStepWith(v.d.a, v.wideA2, wideConst(r), t, s, next, k1);
-    o.next.u = (float)next.u, o.next.w = (float)next.w, o.next.psi = (float)next.psi, o.next.drag = (float)next.drag;
-    o.k1 = (float)k1;
+    o.next.u = narrow(next.u), o.next.w = narrow(next.w), o.next.psi = narrow(next.psi);
+    o.next.drag = narrow(next.drag), o.k1 = narrow(k1);
 }
 
 __device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
                                           StepOut<float>& o) {
     RayState<double> s, next;
-    for (int k = 0; k < 3; ++k) s.n[k] = r.s.n[k], s.v[k] = r.s.v[k];
+    for (int k = 0; k < 3; ++k) s.n[k] = widen(r.s.n[k]), s.v[k] = widen(r.s.v[k]);
     double a1[3];
     polarStepWith(v.wideA2, v.wideTwoA2, wideConst(r), t, s, next, a1);
-    for (int k = 0; k < 3; ++k) o.next.n[k] = (float)next.n[k], o.next.v[k] = (float)next.v[k], o.a1[k] = (float)a1[k];
+    for (int k = 0; k < 3; ++k) o.next.n[k] = narrow(next.n[k]), o.next.v[k] = narrow(next.v[k]), o.a1[k] = narrow(a1[k]);
 }
 
 /* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
@@ -582,6 +618,61 @@ MixedParams paramsOf(const TraceLaunch& l, const void* deviceTable, int viewCoun
 
 }  // namespace
 
+namespace {
+
+/* widen against the hardware's float-to-double conversion, on every float bit pattern (256 a thread);
+ * bad[0] counts differing results (two NaNs agree), bad[2] keeps the least differing input. */
+__global__ void __launch_bounds__(256) checkWiden(unsigned long long* bad) {
+    const uint32_t first = (blockIdx.x * 256u + threadIdx.x) << 8;
+    for (uint32_t k = 0; k < 256u; ++k) {
+        const float f = __uint_as_float(first | k);
+        const double want = (double)f, got = widen(f);
+        const bool same = (want != want && got != got) || __double_as_longlong(want) == __double_as_longlong(got);
+        if (!same) {
+            atomicAdd(bad, 1ull);
+            atomicMin(bad + 2, (unsigned long long)(first | k));
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long mixBits(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* narrow against the hardware's double-to-float conversion, on `perThread` doubles a thread: exponents
+ * around float's range and random fractions, a quarter of them with the 29 bits rounding looks at set
+ * to a tie or next to one, an eighth with the kept bits all ones; one in sixteen a random bit pattern.
+ * bad[1] counts differing results, bad[3] keeps the least differing input. */
+__global__ void __launch_bounds__(256) checkNarrow(unsigned long long* bad, uint32_t perThread) {
+    const unsigned long long id = blockIdx.x * 256ull + threadIdx.x;
+    for (uint32_t k = 0; k < perThread; ++k) {
+        const unsigned long long r = mixBits(id * perThread + k), s = mixBits(r);
+        unsigned long long bits;
+        if ((r & 15u) == 0u) {
+            bits = s;
+        } else {
+            const unsigned long long e = 880u + (r >> 8) % 290u;
+            unsigned long long fraction = s & 0xFFFFFFFFFFFFFull;
+            const uint32_t rests[4] = {0x10000000u, 0x0FFFFFFFu, 0x10000001u, 0u};
+            if (((r >> 4) & 3u) == 0u) fraction = (fraction & ~0x1FFFFFFFull) | rests[(r >> 6) & 3u];
+            if (((r >> 20) & 7u) == 0u) fraction |= 0x7FFFFFull << 29;
+            bits = ((r >> 63) << 63) | (e << 52) | fraction;
+        }
+        const double d = __longlong_as_double((long long)bits);
+        const float want = (float)d, got = narrow(d);
+        const bool same = (want != want && got != got) || __float_as_uint(want) == __float_as_uint(got);
+        if (!same) {
+            atomicAdd(bad + 1, 1ull);
+            atomicMin(bad + 3, bits);
+        }
+    }
+}
+
+}  // namespace
+
 size_t mixedViewBytes() { return sizeof(MixedView); }
 
 int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const ArtfCudaHoleFrame64& frame64,
@@ -667,3 +758,31 @@ cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int 
 }
 
 }  // namespace artf
+
+namespace artf {
+int failWith(int status, const char* message);
+}  // namespace artf
+
+extern "C" int artfCudaCheckConversions(void* stream, uint64_t narrowCount, uint64_t* mismatches) {
+    if (!mismatches) return artf::failWith(ARTF_CUDA_EINVAL, "mismatches is NULL");
+    const cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* bad = nullptr;
+    cudaError_t e = cudaMalloc(&bad, sizeof(unsigned long long) * 4);
+    if (e != cudaSuccess) return artf::failWith(ARTF_CUDA_ENOMEM, "conversion check: device allocation");
+    const unsigned long long init[4] = {0ull, 0ull, ~0ull, ~0ull};
+    e = cudaMemcpyAsync(bad, init, sizeof init, cudaMemcpyHostToDevice, s);
+    const uint32_t threads = 1u << 20;
+    const uint32_t perThread = (uint32_t)((narrowCount + threads - 1) / threads);
+    if (e == cudaSuccess) {
+        artf::checkWiden<<<1u << 16, 256, 0, s>>>(bad); /* 2^24 threads x 256: every float */
+        if (perThread > 0) artf::checkNarrow<<<threads / 256, 256, 0, s>>>(bad, perThread);
+        e = cudaGetLastError();
+    }
+    unsigned long long out[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, bad, sizeof out, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(bad);
+    if (e != cudaSuccess) return artf::failWith(ARTF_CUDA_ELAUNCH, cudaGetErrorString(e));
+    for (int k = 0; k < 4; ++k) mismatches[k] = out[k];
+    return ARTF_CUDA_OK;
+}

@@ -450,6 +450,12 @@ void artfCudaFluidFree(ArtfCudaFluid* f);
 /* The device's FP32 and FP64 fused multiply-add throughput, measured (flop/s, a multiply-add two):
  * the denominators of the trace's roofline.  No reference counterpart.  stream: a cudaStream_t or NULL. */
 int artfCudaProbePeaks(void* stream, int device, double* fp32Flops, double* fp64Flops);
+/* The mixed trace converts between float and double with integer instructions (the FP64 pipe that bounds
+ * it does the hardware's conversions slowly); this checks those against the hardware's conversions:
+ * float to double on every float, double to float on narrowCount doubles around float's range and its
+ * rounding ties.  mismatches[0], [1]: differing results of each (two NaNs agree); [2], [3]: the least
+ * differing input's bits (all ones: none).  Synchronous on `stream` (a cudaStream_t or NULL). */
+int artfCudaCheckConversions(void* stream, uint64_t narrowCount, uint64_t* mismatches);
 
 #ifdef __cplusplus
 }

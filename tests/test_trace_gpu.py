@@ -197,3 +197,13 @@ def test_bad_options_are_refused(lib, ctx):
 
 def capi_einval():
     return -1
+
+
+def test_integer_conversions_match_the_hardware(lib):
+    """The mixed trace's float <-> double conversions on the integer pipe give the hardware's bits: float
+    to double on every float, double to float on 2^28 doubles around float's range and its rounding ties."""
+    import ctypes as C
+    bad = (C.c_uint64 * 4)()
+    capi.check(lib.artfCudaCheckConversions(None, 1 << 28, bad))
+    assert bad[0] == 0, f"float to double: {bad[0]} differ, first {bad[2]:#010x}"
+    assert bad[1] == 0, f"double to float: {bad[1]} differ, first {bad[3]:#018x}"
