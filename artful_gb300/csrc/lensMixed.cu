@@ -89,7 +89,9 @@ struct MixedRay {
  * instruction and one to float two, on the FP64 pipe that bounds this kernel, while the integer pipe
  * idles: these take a handful of integer instructions instead, for the same bits as the hardware's
  * conversions under this unit's flags (flush-to-zero; round to nearest even), NaN aside (a NaN stays a
- * NaN, its payload is not kept).  artfCudaCheckConversions checks them against the hardware's. */
+ * NaN, its payload is not kept).  artfCudaCheckConversions checks them against the hardware's.  The
+ * narrowing is a call, not inlined at its 26 sites in the FP64 paths: inlined, those copies overflowed
+ * the instruction cache (warps stalled waiting for instructions; 3.97 ms against 3.50 at 1080p x 4). */
 __device__ __forceinline__ double widen(float f) {
     const uint32_t b = __float_as_uint(f), sign = b & 0x80000000u, mag = b & 0x7fffffffu, e = mag >> 23;
     uint32_t hi = sign | ((mag >> 3) + 0x38000000u), lo = mag << 29;  /* rebias 127 -> 1023 */
@@ -98,7 +100,7 @@ __device__ __forceinline__ double widen(float f) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
-__device__ __forceinline__ float narrow(double d) {
+__device__ __noinline__ float narrow(double d) {
     const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
     const uint32_t sign = hi & 0x80000000u, e = (hi >> 20) & 0x7ffu;
     /* the top 23 bits of the 52-bit fraction, and the 29 below them that rounding looks at */
