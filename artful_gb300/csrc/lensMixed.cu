@@ -417,6 +417,9 @@ __global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int total
     for (unsigned k = 0; k < planes; ++k) order[at + k] = make_uint2((unsigned)vi | k << 12, tile);
 }
 
+/* FP32 steps a lane takes between two of the warp's votes on refills and FP64 rounds. */
+constexpr int kInnerSteps = 4;
+
 /* This lane's step terms, from the block's table. */
 __device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256]) {
     StepTerms<double> t;
@@ -505,18 +508,8 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         }
         if (__all_sync(full, exhausted && !live)) break;
 
-        /* (2) FP32 steps for the lanes not waiting on FP64 */
-        if (live && !haveStep) {
-            nystromStep(v->f.a, r.c, r.s, o);
-            mixedNeeds(p, *v, r, o, waitR, waitP, reason);
-            haveStep = true;
-            if (waitR || waitP) {
-                ++r.wide;
-                countReason(reason, n);
-            }
-        }
-        /* (3) FP64 rounds, when enough lanes wait or nothing else can move */
-        const unsigned ready = __ballot_sync(full, haveStep && !waitR && !waitP);
+        /* (2) FP64 rounds, when enough lanes wait or no other lane can move */
+        const unsigned ready = __ballot_sync(full, live && !waitR && !waitP);
         const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
         if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
             if (waitR) {
@@ -538,27 +531,41 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         } else if (needP) {
             ++sincePolar;
         }
-        /* (4) commit the steps that are complete */
-        if (haveStep && !waitR && !waitP) {
-            haveStep = false;
-            const unsigned ended = mixedAdvance(p, *v, r, o);
-            if (ended) {
-                const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
-                ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)v->rays + (size_t)k : nullptr;
-                const unsigned rayBits = classBits(mixedFinish(r, ended, end, t));
-                live = false;
-                if (v->rayOut) {
-                    /* (a plane holds the band's pixels) */
-                    const size_t plane = (size_t)v->f.width * (size_t)v->rows;
-                    const size_t inBand = (size_t)(y - v->rowBegin) * (size_t)v->f.width + (size_t)x;
-                    v->rayOut[(size_t)k * plane + inBand] = make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
-                    ++k;
-                } else {
-                    bits |= rayBits;
-                    for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
-                    if (++k == kEnd)
-                        v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share, pixel[2] * v->share,
-                                                    (float)bits);
+        /* (3) up to kInnerSteps FP32 steps a lane between the warp's votes: a lane commits its complete
+         * step (one a round just finished, or a plain one) and takes the next, until a step needs an FP64
+         * sub-step or the ray ends */
+        for (int j = 0; j < kInnerSteps; ++j) {
+            if (haveStep && !waitR && !waitP) {
+                haveStep = false;
+                const unsigned ended = mixedAdvance(p, *v, r, o);
+                if (ended) {
+                    const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
+                    ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)v->rays + (size_t)k : nullptr;
+                    const unsigned rayBits = classBits(mixedFinish(r, ended, end, t));
+                    live = false;
+                    if (v->rayOut) {
+                        /* (a plane holds the band's pixels) */
+                        const size_t plane = (size_t)v->f.width * (size_t)v->rows;
+                        const size_t inBand = (size_t)(y - v->rowBegin) * (size_t)v->f.width + (size_t)x;
+                        v->rayOut[(size_t)k * plane + inBand] =
+                            make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
+                        ++k;
+                    } else {
+                        bits |= rayBits;
+                        for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
+                        if (++k == kEnd)
+                            v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share,
+                                                        pixel[2] * v->share, (float)bits);
+                    }
+                }
+            }
+            if (live && !haveStep) {
+                nystromStep(v->f.a, r.c, r.s, o);
+                mixedNeeds(p, *v, r, o, waitR, waitP, reason);
+                haveStep = true;
+                if (waitR || waitP) {
+                    ++r.wide;
+                    countReason(reason, n);
                 }
             }
         }
