@@ -385,7 +385,7 @@ static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precisio
         stats->flops64 = stats->flops;
     } else if (precision == ARTF_CUDA_MIXED) {
         const bool motion = (guards ? guards : ARTF_CUDA_GUARD_ALL) & ARTF_CUDA_GUARD_MOTION;
-        stats->flops64 = artfFlops64(motion ? stats->rays : 0, stats->fp64Horizon + stats->fp64Radial,
+        stats->flops64 = artfFlops64(motion ? stats->rays : 0, stats->fp64Horizon, stats->fp64Radial,
                                      stats->fp64Polar, frame.spin[0] != 0.f);
     } else {
         stats->flops64 = 0.0;

@@ -319,6 +319,41 @@ ARTF_HD void radialStep(R a, const RayConst<R>& c, const RayState<R>& s, RayStat
     radialStepWith(a, a * a, c, stepTerms(c.step), s, next, k1Out);
 }
 
+/* The radial sub-step's motion alone, u and du/ds, by the same operations as radialStepWith's: the part
+ * a turning point of u concerns (the mixed trace runs it in FP64 there). */
+template <typename R>
+ARTF_HD void radialMotionWith(const RayConst<R>& c, const StepTerms<R>& t, R u, R w, R& nextU, R& nextW, R& k1Out) {
+    const R step = c.step;
+    const R k1 = bendAt(c, u);
+    const R midU = u + t.half * w + t.eighth * k1;
+    const R k2 = bendAt(c, midU);
+    const R endU = u + step * w + t.halfSquare * k2;
+    const R k3 = bendAt(c, endU);
+    nextU = u + step * w + t.sixthSquare * (k1 + (k2 + k2));
+    nextW = w + t.sixth * (k1 + k3 + KF(4.) * k2);
+    k1Out = k1;
+}
+
+/* The polar sub-step's axis component alone, n_z and dn_z/ds, by the same operations as polarStepWith's
+ * for it: n_z'' depends on n_z alone, and the polar turning point is n_z's (the mixed trace runs this in
+ * FP64 there). */
+template <typename R>
+ARTF_HD void polarAxisWith(R a2, R twoA2, const RayConst<R>& c, const StepTerms<R>& t, R nz, R vz, R& nextNz,
+                           R& nextVz, R& a1z) {
+    const R step = c.step;
+    const R c1 = c.big + twoA2 * (nz * nz);
+    const R a1 = a2 * nz - c1 * nz;
+    const R midN = nz + t.half * vz + t.eighth * a1;
+    const R c2 = c.big + twoA2 * (midN * midN);
+    const R a2s = a2 * midN - c2 * midN;
+    const R endN = nz + step * vz + t.halfSquare * a2s;
+    const R c3 = c.big + twoA2 * (endN * endN);
+    const R a3 = a2 * endN - c3 * endN;
+    nextNz = nz + step * vz + t.sixthSquare * (a1 + (a2s + a2s));
+    nextVz = vz + t.sixth * (a1 + a3 + KF(4.) * a2s);
+    a1z = a1;
+}
+
 /* lens.inc:165-192, the polar part: n on the sphere and dn/ds, with the step's terms, a2 = a * a and
  * twoA2 = 2 * a2 given. */
 template <typename R>

@@ -32,18 +32,21 @@
 /* The mixed trace's FP64 work, by the same rule, for the FP64 pipe's roofline:
  *   per set-up   a ray's constants of motion and first state (what it takes from its view formed once a
  *                view), and its step's terms (formed once a ray)
- *   per radial   one radial sub-step (u, du/ds and psi) with those terms given; spin 0: no drag, no psi
- *   per polar    one polar sub-step (n, dn/ds) */
+ *   per horizon  one whole radial sub-step (u, du/ds and psi) with those terms given, in the horizon's
+ *                band; spin 0: no drag, no psi
+ *   per turn     the radial motion alone (u, du/ds), at a turning point of u
+ *   per polar    the polar axis component alone (n_z, dn_z/ds), at a turning point of n_z */
 #define ARTF_FLOPS_WIDE_START 66
 #define ARTF_FLOPS_WIDE_RADIAL 61
 #define ARTF_FLOPS_WIDE_RADIAL_SPINLESS 34
-#define ARTF_FLOPS_WIDE_POLAR 87
+#define ARTF_FLOPS_WIDE_TURN 34
+#define ARTF_FLOPS_WIDE_AXIS 37
 
-static inline double artfFlops64(unsigned long long setups, unsigned long long radial, unsigned long long polar,
-                                 int spinning) {
+static inline double artfFlops64(unsigned long long setups, unsigned long long horizon, unsigned long long turns,
+                                 unsigned long long polar, int spinning) {
     return ARTF_FLOPS_WIDE_START * (double)setups +
-           (spinning ? ARTF_FLOPS_WIDE_RADIAL : ARTF_FLOPS_WIDE_RADIAL_SPINLESS) * (double)radial +
-           ARTF_FLOPS_WIDE_POLAR * (double)polar;
+           (spinning ? ARTF_FLOPS_WIDE_RADIAL : ARTF_FLOPS_WIDE_RADIAL_SPINLESS) * (double)horizon +
+           ARTF_FLOPS_WIDE_TURN * (double)turns + ARTF_FLOPS_WIDE_AXIS * (double)polar;
 }
 
 static inline double artfFlops(unsigned long long rays, unsigned long long steps, unsigned long long crossings,

@@ -6,10 +6,11 @@
  *   HORIZON  within a band of the outer horizon (u > band * 0.995 / r+) the radial sub-step of
  *            (u, du/ds, psi) runs in FP64: Delta / r^2 in the frame-drag rate loses most of its bits to
  *            cancellation there;
- *   RADIAL   the step in which du/ds changes sign (the radial potential's zero) has its radial
- *            sub-step in FP64;
+ *   RADIAL   the step in which du/ds changes sign (the radial potential's zero) has its motion of
+ *            (u, du/ds) in FP64 (psi and its rate, smooth there, stay the FP32 step's);
  *   POLAR    the step in which the axis part of dn/ds changes sign (the polar potential's zero) has
- *            its polar sub-step of (n, dn/ds) in FP64;
+ *            the axis component (n_z, dn_z/ds) in FP64: n_z'' depends on n_z alone, and the turning
+ *            point is its (the components about the axis stay the FP32 step's);
  *   PSI      psi, the frame-drag angle, is summed with a compensated (two-sum) accumulator, and the
  *            endpoint's Mino time is formed in FP64 from the step count: neither drifts over 192 steps.
  * The radial and polar sub-steps are independent (u'' depends on u alone, n'' on n alone), so a guard
@@ -171,24 +172,34 @@ __device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedView
     reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
 }
 
-/* The FP64 sub-steps, with the ray's step terms (stepTerms(r.step), formed once a ray). */
+/* The FP64 sub-steps, with the ray's step terms (stepTerms(r.step), formed once a ray).  Radial: in the
+ * horizon's band the whole sub-step (the frame-drag rate's Delta / r^2 cancels there); at a turning point
+ * of u the motion (u, du/ds) alone, psi and its rate staying the FP32 step's. */
 __device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
-                                           StepOut<float>& o) {
-    RayState<double> s, next;
-    s.u = widen(r.s.u), s.w = widen(r.s.w), s.psi = 0.0, s.drag = widen(r.s.drag);
+                                           bool band, StepOut<float>& o) {
+    const RayConst<double> c = wideConst(r);
     double k1;
-    radialStepWith(v.d.a, v.wideA2, wideConst(r), t, s, next, k1);
-    o.next.u = narrow(next.u), o.next.w = narrow(next.w), o.next.psi = narrow(next.psi);
-    o.next.drag = narrow(next.drag), o.k1 = narrow(k1);
+    if (band) {
+        RayState<double> s, next;
+        s.u = widen(r.s.u), s.w = widen(r.s.w), s.psi = 0.0, s.drag = widen(r.s.drag);
+        radialStepWith(v.d.a, v.wideA2, c, t, s, next, k1);
+        o.next.u = narrow(next.u), o.next.w = narrow(next.w), o.next.psi = narrow(next.psi);
+        o.next.drag = narrow(next.drag);
+    } else {
+        double u, w;
+        radialMotionWith(c, t, widen(r.s.u), widen(r.s.w), u, w, k1);
+        o.next.u = narrow(u), o.next.w = narrow(w);
+    }
+    o.k1 = narrow(k1);
 }
 
+/* Polar: at the turning point of n_z, the axis component (n_z, dn_z/ds); the components about the axis
+ * stay the FP32 step's. */
 __device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
                                           StepOut<float>& o) {
-    RayState<double> s, next;
-    for (int k = 0; k < 3; ++k) s.n[k] = widen(r.s.n[k]), s.v[k] = widen(r.s.v[k]);
-    double a1[3];
-    polarStepWith(v.wideA2, v.wideTwoA2, wideConst(r), t, s, next, a1);
-    for (int k = 0; k < 3; ++k) o.next.n[k] = narrow(next.n[k]), o.next.v[k] = narrow(next.v[k]), o.a1[k] = narrow(a1[k]);
+    double nz, vz, a1z;
+    polarAxisWith(v.wideA2, v.wideTwoA2, wideConst(r), t, widen(r.s.n[2]), widen(r.s.v[2]), nz, vz, a1z);
+    o.next.n[2] = narrow(nz), o.next.v[2] = narrow(vz), o.a1[2] = narrow(a1z);
 }
 
 /* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
@@ -287,7 +298,7 @@ __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const Mi
         mixedNeeds(p, v, r, o, radial, polar, reason);
         if (radial || polar) {
             const StepTerms<double> terms = stepTerms(r.step);
-            if (radial) radialWide(v, r, terms, o);
+            if (radial) radialWide(v, r, terms, (reason & 1u) != 0u, o);
             if (polar) polarWide(v, r, terms, o);
         }
         if (radial || polar) {
@@ -513,7 +524,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
         const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
         if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
             if (waitR) {
-                radialWide(*v, r, laneTerms(terms), o);
+                radialWide(*v, r, laneTerms(terms), (reason & 1u) != 0u, o);
                 waitR = false;
             }
             sinceRadial = 0;

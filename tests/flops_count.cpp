@@ -100,7 +100,15 @@ int main() {
             printf("wide_radial%s %ld\n", tag, g_ops);
             g_ops = 0;
             polarStepWith(a2, twoA2, cw, terms, sw, next, a1);
-            printf("wide_polar%s %ld\n", tag, g_ops);
+            printf("wide_polar_whole%s %ld\n", tag, g_ops);
+            /* what the turning-point guards run: the radial motion alone, the polar axis component alone */
+            Op nu, nw, nz, vz, a1z;
+            g_ops = 0;
+            radialMotionWith(cw, terms, sw.u, sw.w, nu, nw, k1);
+            printf("wide_turn%s %ld\n", tag, g_ops);
+            g_ops = 0;
+            polarAxisWith(a2, twoA2, cw, terms, sw.n[2], sw.v[2], nz, vz, a1z);
+            printf("wide_axis%s %ld\n", tag, g_ops);
         }
         /* one Nystrom step as written: each sub-step recomputes the ray's constant products */
         StepOut<Op> o;

@@ -62,8 +62,12 @@ def test_per_escape(counts, constants):
 
 def test_mixed_fp64_work(counts, constants):
     """The mixed trace's FP64 pipe work: a ray's set-up with its view's terms given (and its step's terms
-    formed), and one radial and one polar sub-step with those terms given."""
+    formed), a whole radial sub-step (the horizon's band), the radial motion alone (a turning point of u)
+    and the polar axis component alone (a turning point of n_z), with those terms given."""
     assert constants["WIDE_START"] == counts["wide_start"] == counts["wide_start_spinless"]
     assert constants["WIDE_RADIAL"] == counts["wide_radial"]
     assert constants["WIDE_RADIAL_SPINLESS"] == counts["wide_radial_spinless"]
-    assert constants["WIDE_POLAR"] == counts["wide_polar"] == counts["wide_polar_spinless"]
+    assert constants["WIDE_TURN"] == counts["wide_turn"] == counts["wide_turn_spinless"]
+    assert constants["WIDE_AXIS"] == counts["wide_axis"] == counts["wide_axis_spinless"]
+    # each part is a subset of its whole sub-step's operations
+    assert counts["wide_axis"] < counts["wide_polar_whole"] and counts["wide_turn"] < counts["wide_radial"]
