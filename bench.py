@@ -40,9 +40,9 @@ UNIT = "geodesics/s"
 # Kernels one mixed frame launches: the tile probe, the heavy-first order, the trace, the ray-plane sum.
 LAUNCHES_PER_MIXED_FRAME = 4
 # DRAM bytes (read + write) of one launch of the mixed trace kernel at this workload, from one ncu
-# capture (dram__bytes_read.sum 17.78 MB + dram__bytes_write.sum 74.55 MB): the map read once, and the
+# capture (dram__bytes_read.sum 17.14 MB + dram__bytes_write.sum 74.06 MB): the map read once, and the
 # part of the 133 MB of ray planes that leaves L2 before the sum reads it back.
-TRACE_TRAFFIC_BYTES = 92_330_000
+TRACE_TRAFFIC_BYTES = 91_200_000
 
 
 def parse():
