@@ -70,6 +70,8 @@ struct ArtfCuda {
     double* adjResults;
     double* adjResultsHost;
     size_t adjResultViews;
+    void* adjOrder;               /* the adjoint's heavy-first tile order (artf::adjointOrderBytes) */
+    size_t adjOrderBytes;
     uint32_t lastBands; /* launches of the last trace (1 but for a frame in bands) */
     int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
     bool lost;
@@ -154,6 +156,7 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->adjPartials);
     cudaFree(ctx->adjResults);
     cudaFreeHost(ctx->adjResultsHost);
+    cudaFree(ctx->adjOrder);
     if (ctx->start) cudaEventDestroy(ctx->start);
     if (ctx->stop) cudaEventDestroy(ctx->stop);
     if (ctx->staged) cudaEventDestroy(ctx->staged);
@@ -620,7 +623,7 @@ extern "C" int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* par
 }
 
 /* Grows the adjoint's table, staging, block sums and results to `count` views of `blocks` blocks. */
-static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks) {
+static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int height) {
     if ((size_t)count > ctx->adjViews) {
         cudaFree(ctx->adjTable);
         cudaFreeHost(ctx->adjStage);
@@ -639,7 +642,9 @@ static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks) {
         CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->adjResultsHost, sizeof(double) * 8 * count));
         ctx->adjResultViews = (size_t)count;
     }
-    return reserve((void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float));
+    if (int s = reserve((void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float)))
+        return s;
+    return reserve(&ctx->adjOrder, &ctx->adjOrderBytes, artf::adjointOrderBytes(count, width, height), 1);
 }
 
 extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
@@ -658,7 +663,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
                     ARTF_CUDA_ADJOINT_MIN_CHECKPOINT, ARTF_CUDA_ADJOINT_MAX_CHECKPOINT);
     if ((!map && !ctx->mapHeld) || (!fluid && !ctx->fluidHeld)) return fail(ARTF_CUDA_EINVAL, "no map or fluid");
     const int pixels = width * height, blocks = artf::adjointTiles(width, height);
-    if ((status = reserveAdjoint(ctx, count, blocks))) return status;
+    if ((status = reserveAdjoint(ctx, count, blocks, width, height))) return status;
     /* (the staging is free: every call ends synchronised) */
     const size_t slot = artf::adjointViewBytes();
     for (int v = 0; v < count; ++v) {
@@ -678,7 +683,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
     const cudaError_t e = artf::launchAdjoint(ctx->adjTable, count, width, height, checkpointEvery, ctx->counters,
-                                              ctx->adjPartials, ctx->adjResults, ctx->stream);
+                                              ctx->adjPartials, ctx->adjResults, ctx->stream, ctx->adjOrder);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "adjoint launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(ctx->adjResultsHost, ctx->adjResults, sizeof(double) * 8 * count,

@@ -682,6 +682,7 @@ struct AdjointLaunch {
     const AdjointView* views;
     float* partials; /* 8 floats a tile: the loss, the five gradient components, two unused */
     unsigned long long* counters;
+    const int* order; /* each view's tiles, heaviest first (tilesPerView a view), or NULL: in order */
     int tilesX, tilesPerView, totalTiles, K;
 };
 
@@ -815,8 +816,9 @@ __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L)
     }
     __syncthreads();
     const int lane = (int)(threadIdx.x & 31);
-    const int local = (int)(blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5));
-    if (local >= L.tilesPerView) return; /* the whole warp: its tile lies past the view */
+    const int slot = (int)(blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5));
+    if (slot >= L.tilesPerView) return; /* the whole warp: its tile lies past the view */
+    const int local = L.order ? L.order[(size_t)blockIdx.y * L.tilesPerView + slot] : slot;
     const int px = (local % L.tilesX) * 8 + (lane & 7), py = (local / L.tilesX) * 4 + (lane >> 3);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     Tally tally;
@@ -829,6 +831,74 @@ __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L)
         for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
         if (lane == 0) L.partials[tile * 8 + k] = s;
     }
+}
+
+/* ---- heavy tiles first ----------------------------------------------------------------------------
+ * Blocks are dispatched in order and a ray's adjoint costs in proportion to its steps, so the heaviest
+ * tiles go to the first blocks: the launch does not end on a few photon-ring tiles while the rest of the
+ * GPU idles.  A tile's weight is the step count of one FP32 ray through its middle, up to 64 steps, in
+ * classes of 8; a counting sort a view orders the tiles.  Each tile still writes its own partial sums and
+ * adjointSums adds them in tile order, so the gradients are the same bits in any order. */
+constexpr int kAdjointClasses = 9;
+constexpr int kClassStride = 16; /* a view's class counters */
+
+__global__ void __launch_bounds__(128) adjointProbe(const AdjointLaunch L, int* weights, unsigned* classes) {
+    __shared__ unsigned counts[kAdjointClasses];
+    if (threadIdx.x < kAdjointClasses) counts[threadIdx.x] = 0;
+    __syncthreads();
+    const int local = (int)(blockIdx.x * 128 + threadIdx.x);
+    if (local < L.tilesPerView) {
+        const AdjointView& v = L.views[blockIdx.y];
+        const int px = min((local % L.tilesX) * 8 + 4, v.f.width - 1);
+        const int py = min((local / L.tilesX) * 4 + 2, v.f.height - 1);
+        float nx, ny, moment;
+        samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
+        RayConst<float> c;
+        RayState<float> s;
+        rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
+        const float a = v.f.a;
+        if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
+        int i = 0;
+        while (i < 64) {
+            StepOut<float> o;
+            nystromStep(a, c, s, o);
+            ++i;
+            if (0.f > o.next.u || o.next.u > v.f.uHorizon) break;
+            s = o.next;
+        }
+        const int w = min(i >> 3, kAdjointClasses - 1);
+        weights[(size_t)blockIdx.y * L.tilesPerView + local] = w;
+        atomicAdd(counts + w, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kAdjointClasses && counts[threadIdx.x])
+        atomicAdd(classes + blockIdx.y * kClassStride + threadIdx.x, counts[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(128) adjointPlace(const AdjointLaunch L, const int* weights, const unsigned* classes,
+                                                    unsigned* cursors, int* order) {
+    __shared__ unsigned counts[kAdjointClasses], runs[kAdjointClasses];
+    if (threadIdx.x < kAdjointClasses) counts[threadIdx.x] = 0;
+    __syncthreads();
+    const int local = (int)(blockIdx.x * 128 + threadIdx.x);
+    const bool active = local < L.tilesPerView;
+    int w = 0;
+    unsigned within = 0;
+    if (active) {
+        w = weights[(size_t)blockIdx.y * L.tilesPerView + local];
+        within = atomicAdd(counts + w, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kAdjointClasses) {
+        const unsigned* mine = classes + blockIdx.y * kClassStride;
+        unsigned before = 0;
+        for (int c = kAdjointClasses - 1; c > (int)threadIdx.x; --c) before += mine[c];
+        runs[threadIdx.x] = counts[threadIdx.x]
+                                ? before + atomicAdd(cursors + blockIdx.y * kClassStride + threadIdx.x, counts[threadIdx.x])
+                                : 0u;
+    }
+    __syncthreads();
+    if (active) order[(size_t)blockIdx.y * L.tilesPerView + runs[w] + within] = local;
 }
 
 /* One block a view: its tiles' sums added in double, in a fixed order. */
@@ -875,16 +945,33 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
     memcpy(slot, &v, sizeof v);
 }
 
+size_t adjointOrderBytes(int count, int width, int height) {
+    return sizeof(unsigned) * 2 * kClassStride * (size_t)count + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
+}
+
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
-                          float* partials, double* results, cudaStream_t stream) {
+                          float* partials, double* results, cudaStream_t stream, void* orderScratch) {
     AdjointLaunch L;
     L.views = (const AdjointView*)table;
     L.partials = partials;
     L.counters = counters;
+    L.order = nullptr;
     L.tilesX = (width + 7) / 8;
     L.tilesPerView = adjointTiles(width, height);
     L.totalTiles = L.tilesPerView * count;
     L.K = K;
+    if (orderScratch) {
+        unsigned* classes = (unsigned*)orderScratch;
+        unsigned* cursors = classes + kClassStride * (size_t)count;
+        int* weights = (int*)(cursors + kClassStride * (size_t)count);
+        int* order = weights + (size_t)count * L.tilesPerView;
+        const cudaError_t e = cudaMemsetAsync(orderScratch, 0, sizeof(unsigned) * 2 * kClassStride * (size_t)count, stream);
+        if (e != cudaSuccess) return e;
+        const dim3 grid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
+        adjointProbe<<<grid, 128, 0, stream>>>(L, weights, classes);
+        adjointPlace<<<grid, 128, 0, stream>>>(L, weights, classes, cursors, order);
+        L.order = order;
+    }
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
     adjointPixels<<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
     adjointSums<<<count, 256, 0, stream>>>(partials, L.tilesPerView, results);

@@ -33,6 +33,8 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
 /* The adjoint over `count` views of width x height; partials: count * adjointTiles(width, height) * 8
  * floats of scratch; results: count * 8 doubles (the loss, the five gradient components, two unused). */
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
-                          float* partials, double* results, cudaStream_t stream);
+                          float* partials, double* results, cudaStream_t stream, void* orderScratch);
+/* Device bytes of the adjoint's heavy-first tile order (orderScratch above; NULL: the tiles in order). */
+size_t adjointOrderBytes(int count, int width, int height);
 
 }  // namespace artf
