@@ -3,7 +3,8 @@
  * distance), carried through the trace's own templated core in dual numbers (lensDual.cuh).  The frame's
  * fields enter with their derivatives (the Jacobian of the frame in the parameters), the emissivity
  * index as the fourth direction, and the two parameter-dependent map tables from their formulas.
- * One thread a pixel, one ray at its centre; slow (five tangents in double) and exact: a checker. */
+ * One thread a pixel, one ray at its centre; slow (five tangents in double) and exact: a reference for
+ * the adjoint's gradients to be checked against. */
 #include "lensDual.cuh"
 #include "lensKernel.cuh"
 #include "lensTangent.h"

@@ -1,6 +1,6 @@
 """Python access to the oracle (oracle/liboracle.so) and, where it has been built from the reference's
 sources, to the reference itself (oracle/_ref/libartref.so).  Test infrastructure: only tests/,
-__graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the checker.
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it, to check results and to time the CPU.
 """
 from __future__ import annotations
 

@@ -1,4 +1,4 @@
-/* Oracle (test infrastructure, the checker): the reference's painted disc map, src/scene/hole.c:14-197
+/* Oracle (test infrastructure): the reference's painted disc map, src/scene/hole.c:14-197
  * (buildDisc and setRings), restated in scalar C.  Only tests/ use it, to check the GPU painter
  * (artful_gb300/csrc/disc.cu) byte for byte; it is pinned against the reference's own map (oracle/_ref,
  * refMap) and against the golden hash in tests/golden/.

@@ -1,4 +1,4 @@
-/* Oracle (test infrastructure, the checker): the reference's disc fluid, src/scene/fluid.c, restated in
+/* Oracle (test infrastructure): the reference's disc fluid, src/scene/fluid.c, restated in
  * scalar C on one thread.  Only tests/ use it, to check the GPU fluid step (artful_gb300/csrc/fluid.cu)
  * byte for byte; it is pinned in turn against the reference's own fluid.c (oracle/_ref, refFluid*) and
  * against the golden hashes in tests/golden/.

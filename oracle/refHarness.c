@@ -1,5 +1,5 @@
 /* Test-only harness around the reference renderer, built from the reference's own sources by
- * oracle/ref.mk into oracle/_ref/libartref.so.  It is the checker's checker: the oracle restatement
+ * oracle/ref.mk into oracle/_ref/libartref.so.  It pins the oracle: the oracle restatement
  * (oracle/lensOracle.c) and the golden fixtures under tests/golden/ are pinned against what these
  * entry points return.  Nothing in the product links or loads it.
  *

@@ -53,6 +53,6 @@ def ctx(lib):
     handle = C.c_void_p()
     status = lib.artfCudaCreate(0, C.byref(handle))
     if status != 0:
-        pytest.fail(f"artfCudaCreate failed on the GPU box: {lib.artfCudaLastError().decode()}")
+        pytest.fail(f"artfCudaCreate failed on this GPU: {lib.artfCudaLastError().decode()}")
     yield handle
     lib.artfCudaDestroy(handle)
