@@ -266,13 +266,40 @@ def cpu_baseline(scene, frame, map_, fluid, jitter, budget_s=12.0):
     total = int(min(scene.height, max(8, budget_s * rays_per_s / (scene.width * jitter))))
     y0 = max(0, scene.height // 2 - total // 2)
     t0 = time.perf_counter()
-    binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads,
-                     rows=(y0, y0 + total))
+    hdr = binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads,
+                           rows=(y0, y0 + total))
     dt = time.perf_counter() - t0
     return {"value": total * scene.width * jitter / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"rows {y0}..{y0 + total} of the 1920x1080 frame, {jitter} jittered rays a pixel "
                       f"({total * scene.width * jitter} geodesics, {dt:.1f} s); the oracle port, scalar C, "
-                      f"{threads} threads"}
+                      f"{threads} threads"}, hdr[y0:y0 + total], (y0, y0 + total)
+
+
+def vs_reference_cpu(gpu, cpu, rows):
+    """The GPU frame against the reference's CPU trace of the same rays (the oracle port, the reference's
+    bits): pixel classes (disc / sky / horizon) outside one pixel of the photon ring, and the radiance's
+    relative error (of the RGB sum, floor 1e-3)."""
+    bits_gpu = gpu[rows[0]:rows[1], :, 3].astype(np.uint32)
+    bits_cpu = cpu[..., 3].astype(np.uint32)
+    dark = (bits_cpu & 3) == 0
+    near = np.zeros_like(dark)
+    padded = np.pad(dark, 1, mode="edge")
+    h, w = dark.shape
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            near |= padded[1 + dy:1 + dy + h, 1 + dx:1 + dx + w] != dark
+    keep = ~near
+
+    def classes(b):
+        return np.where(b & 1, 1, np.where(b & 2, 2, 0))
+
+    agree = float(np.mean(classes(bits_gpu)[keep] == classes(bits_cpu)[keep]))
+    a = gpu[rows[0]:rows[1], :, :3].astype(np.float64).sum(-1)
+    b = cpu[..., :3].astype(np.float64).sum(-1)
+    rel = (np.abs(a - b) / np.maximum(np.abs(b), 1e-3))[keep]
+    return {"rows": list(rows), "class_agreement_outside_ring": agree, "ring_share": float(near.mean()),
+            "radiance_within_1e-3": float(np.mean(rel <= 1e-3)), "radiance_rel_p99": float(np.quantile(rel, 0.99)),
+            "reference": "the oracle port, the reference's lensTrace bit for bit"}
 
 
 def run_reference(args, rank, world):
@@ -429,7 +456,8 @@ def main():
     batch = None
     adjoint = fitting = next_rows = None
     if rank == 0 and not args.quick:
-        cpu = cpu_baseline(scene, frame, map_, fluid, rays)
+        cpu, cpu_rows, rows = cpu_baseline(scene, frame, map_, fluid, rays)
+        versus_cpu = vs_reference_cpu(img_mixed, cpu_rows, rows)
         batch = batch_measurement(lib, ctx, args.steps, flush)
         adjoint = adjoint_measurement(lib, ctx, args.steps, flush)
         fitting = fit_measurement(lib, ctx, args.fd_fits)
@@ -466,6 +494,7 @@ def main():
     }
     if cpu:
         line["cpu_baseline"] = cpu
+        line["mixed_vs_reference_cpu"] = versus_cpu
     if batch:
         line["batch_64_views"] = batch
     if adjoint:
