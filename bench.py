@@ -408,7 +408,8 @@ def main():
         ms = timed(prec, args.steps, 1)
         s = stats_of(prec)
         side[name] = {"geodesics_per_s": geodesics / (ms * 1e-3), "ms_per_frame": ms,
-                      "steps_per_s": s.steps / (ms * 1e-3)}
+                      "steps_per_s": s.steps / (ms * 1e-3), "flops_per_frame": s.flops}
+    side["fp64"]["flops_per_frame"] = stats_of(capi.FP64).flops
 
     # endpoint error of the mixed trace: against FP64 at the same step (precision) and at half step
     # (precision and discretisation), over every ray of the frame
@@ -436,6 +437,10 @@ def main():
     peak = fp32_peak.value / 1e12
     achieved64 = s_mixed.flops64 / (ms_mixed * 1e-3) / 1e12
     peak64 = fp64_peak.value / 1e12
+    # the other traces against their own pipe: FP32 (exact, fast) and FP64 (plain), of the measured peaks
+    for name, pipe_peak in (("fp32_exact", peak), ("fp32_fast", peak), ("fp64", peak64)):
+        entry = side[name]
+        entry["pipe_frac"] = entry["flops_per_frame"] / (entry["ms_per_frame"] * 1e-3) / 1e12 / pipe_peak
 
     # end to end through the host-buffer entry point
     pin_map = torch.from_numpy(map_).pin_memory()
