@@ -631,7 +631,8 @@ MixedParams paramsOf(const TraceLaunch& l, const void* deviceTable, int viewCoun
     p.guards = l.guards ? l.guards : ARTF_CUDA_GUARD_ALL;
     p.batch = l.fp64Batch > 0 ? (l.fp64Batch > 32 ? 32 : l.fp64Batch) : 32;
     p.refill = l.refillBatch > 0 ? (l.refillBatch > 32 ? 32 : l.refillBatch) : 32;
-    p.maxWait = l.compactEvery > 0 ? l.compactEvery : 64;
+    /* (256 votes: the best of the autotuner's choices on both the 1080p frame and the 64-view batch) */
+    p.maxWait = l.compactEvery > 0 ? l.compactEvery : 256;
     p.order = nullptr;
     return p;
 }
