@@ -110,7 +110,7 @@ def sweep(args):
                       "vs_fp64_half": endpoint_error(e32, e64h, img32, img64h)}), flush=True)
     G = capi
     variants = [
-        ("defaults: all guards, band 0.8, batch 32, refill 16, wait 64, block 128", dict()),
+        ("defaults: all guards, band 0.8, batch 32, refill 32, wait 256, block 128", dict()),
         ("band 0.5", dict(band=0.5)),
         ("band 0.9", dict(band=0.9)),
         ("batch 16", dict(batch=16)),
