@@ -673,7 +673,7 @@ __device__ void startBack(const AdjointView& v, float nx, float ny, const RayCon
 
 /* ---- the kernels -------------------------------------------------------------------------------- */
 
-struct Kept {
+struct alignas(16) Kept {
     RayState<float> s;
     float through; /* the disc's transmission before this step's crossing */
 };
@@ -715,7 +715,7 @@ __device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py,
     Kept checkpoint[kMaxSegments];
     /* forward: the segment's states, and each segment's first */
     float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
-    int steps = 0;
+    int steps = 0, lastCrossing = -1;
     unsigned crossings = 0;
     bool escaped = false;
     RayState<float> end = s;
@@ -723,7 +723,9 @@ __device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py,
         if (step % K == 0) checkpoint[step / K] = Kept{s, through};
         ring[step % K] = Kept{s, through};
         StepOut<float> o;
+        const unsigned crossed = crossings;
         stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
+        if (crossings != crossed) lastCrossing = step;
         ++steps;
         end = o.next;
         if (0.f > o.next.u) {
@@ -752,9 +754,16 @@ __device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py,
     ConstBar g;
     memset(&g, 0, sizeof g);
     float throughBar = 0.f;
-    for (int first = lastFirst; first >= 0; first -= K) {
-        const int last = min(first + K, steps); /* steps first .. last - 1 */
-        RayState<float> after = end;            /* the state at the segment's end */
+    /* Back from the last step that added to the radiance (the escape, when the sky is shown; else the last
+     * disc crossing): after it every adjoint is zero, and a step taken back with zero adjoints adds exactly
+     * nothing, so those steps, and the recomputation of segments holding only them, are skipped. */
+    const int top = escaped && f.stars > 0.f ? steps : lastCrossing + 1; /* steps 0 .. top - 1 go back */
+    for (int first = top > 0 ? ((top - 1) / K) * K : -K; first >= 0; first -= K) {
+        const int last = min(first + K, top); /* steps first .. last - 1 */
+        /* the state at the segment's end: the ray's, the start of step `last` (in the ring when this is the
+         * ray's last segment), or where the recomputation ends */
+        RayState<float> after = end;
+        if (first == lastFirst && last != steps) after = ring[last - first].s;
         if (first != lastFirst) {
             RayState<float> r = checkpoint[first / K].s;
             float t = checkpoint[first / K].through, junk[3] = {0.f, 0.f, 0.f};

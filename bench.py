@@ -513,11 +513,15 @@ def main():
 
 def _median_ms(run, steps, flush=None):
     """Median over `steps` runs of the device time a run reports (its own CUDA events), after a flush of L2
-    before each when a flush buffer is given."""
+    before each when a flush buffer is given.  The flush runs on torch's stream and the library's launches
+    on the context's own (non-blocking) stream, so the flush is waited for: overlapping the timed launch
+    it would slow it."""
+    import torch
     times = []
     for _ in range(max(3, steps)):
         if flush is not None:
             flush.fill_(1)
+            torch.cuda.synchronize()
         times.append(run())
     return statistics.median(times)
 
