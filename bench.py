@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "geodesics/s @1080p: mixed-prec vs FP64 GPU at ≤1e-4 endpoint err; adj/fwd time"
 UNIT = "geodesics/s"
+WORKLOAD = "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50 M, i=85 deg, disc ISCO..12 M r^-3, 2000 stars"
 # Kernels one mixed frame launches: the tile probe, the heavy-first order, the trace, the ray-plane sum.
 LAUNCHES_PER_MIXED_FRAME = 4
 # DRAM bytes (read + write) of one launch of the mixed trace kernel at this workload, from one ncu
@@ -325,8 +326,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows * scene.width * 4 / value * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50, i=85",
-                       "sample_per_step": f"{rows} rows x 1920 x 4 rays"},
+            "config": {"workload": WORKLOAD, "sample_per_step": f"{rows} rows x 1920 x 4 rays"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{rows} rows of the frame a step; the reference's sources are not on "
                                        "this host, so its algorithm runs as the oracle port (scalar C)"},
@@ -476,8 +476,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50 M, i=85 deg, "
-                               "disc ISCO..12 M r^-3, 2000 stars", "precision": "mixed",
+        "config": {"workload": WORKLOAD, "precision": "mixed",
                    "parallelism": f"replicas{world}", "l2": "flushed (256 MB write) before every timed step"},
         "mixed_over_fp64": side["fp64"]["ms_per_frame"] / ms_mixed,
         "steps_per_s": s_mixed.steps / (ms_mixed * 1e-3) * world,
