@@ -836,10 +836,14 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
     }
     cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaMemcpyAsync(g->table, g->stage, bytes, cudaMemcpyHostToDevice, ctx->stream);
-        cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
-        artf::launchMixedTable(l, g->table, count, g->units, g->combine, g->tiles, g->order);
+        /* (a failed call ends the capture all the same, so the stream is left out of capture mode) */
+        cudaError_t captured = cudaMemcpyAsync(g->table, g->stage, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (captured == cudaSuccess)
+            captured = cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
+        if (captured == cudaSuccess)
+            captured = artf::launchMixedTable(l, g->table, count, g->units, g->combine, g->tiles, g->order);
         e = cudaStreamEndCapture(ctx->stream, &g->graph);
+        if (e == cudaSuccess && captured != cudaSuccess) e = captured;
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
     if (e != cudaSuccess) {
