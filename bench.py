@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--views", type=int, default=1, help="views of --profile adjoint")
+    p.add_argument("--guards", type=int, default=0,
+                   help="the mixed trace's FP64 guards for --profile mixed (ARTF_CUDA_GUARD_* bits; 0: all)")
+    p.add_argument("--persistent", action="store_true", help="the persistent form of --profile exact/fp32/fp64")
     p.add_argument("--sweep", action="store_true",
                    help="time the mixed trace's guard, band and batch variants, each with its endpoint error")
     p.add_argument("--fd-fits", type=int, default=4,
@@ -169,7 +172,8 @@ def profile_case(args):
     unit = scenes.unit_fluid()  # (kept alive across the call: the ABI reads it)
     capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 1))
     hdr = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
-    o = capi.TraceOptions(capi.PRECISIONS[args.profile], 4, scene.jitter_seed, 1.0, 0.0, 0, 0, 0)
+    o = capi.TraceOptions(capi.PRECISIONS[args.profile], 4, scene.jitter_seed, 1.0, 0.0, 0, 0,
+                          1 if args.persistent else 0, args.guards)
     for _ in range(2):
         s = capi.TraceStats()
         capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
