@@ -420,7 +420,8 @@ static int launchBand(ArtfCuda* ctx, artf::TraceLaunch& l, int precision) {
                                               np ? ctx->planes : nullptr, 0, 0, ctx->stage, &tiles);
         if (int s = reserveOrder(ctx, tiles, units)) return s;
         if (int s = sendTable(ctx, 1)) return s;
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0, tiles, ctx->order);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, 1, units, np ? pixels : 0, tiles, ctx->order,
+                                                     ctx->stage);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "mixed trace launch: %s", cudaGetErrorString(e));
         return ARTF_CUDA_OK;
     }
@@ -769,7 +770,8 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     if ((status = sendTable(ctx, count))) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order);
+    const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order,
+                                                     count == 1 ? ctx->stage : nullptr);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
@@ -841,7 +843,8 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
         if (captured == cudaSuccess)
             captured = cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream);
         if (captured == cudaSuccess)
-            captured = artf::launchMixedTable(l, g->table, count, g->units, g->combine, g->tiles, g->order);
+            captured = artf::launchMixedTable(l, g->table, count, g->units, g->combine, g->tiles, g->order,
+                                              nullptr); /* (an update rewrites the table, not a captured copy) */
         e = cudaStreamEndCapture(ctx->stream, &g->graph);
         if (e == cudaSuccess && captured != cudaSuccess) e = captured;
     }
@@ -900,7 +903,8 @@ static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int u
         CUDA_OR(ARTF_CUDA_ELAUNCH,
                 cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
-        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order);
+        const cudaError_t e = artf::launchMixedTable(l, ctx->table, count, units, combine, tiles, ctx->order,
+                                                     count == 1 ? ctx->stage : nullptr);
         if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "autotune launch: %s", cudaGetErrorString(e));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventSynchronize(ctx->stop));

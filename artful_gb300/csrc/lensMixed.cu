@@ -439,8 +439,9 @@ __device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256
     return t;
 }
 
-/* The warp-scheduled trace (see the file's head). */
-__global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
+/* The warp-scheduled trace (see the file's head).  kOne: a single view, read from `one` (a kernel
+ * parameter) rather than from the view table. */
+template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView* one) {
     /* each lane's ray's step terms in double, formed at its set-up: an FP64 round then loads them
      * where it would multiply them out again (FP64 multiplies are the scarce resource) */
     __shared__ double terms[5][256];
@@ -450,7 +451,7 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     Tally t;
     Reasons n;
     int unit = -1, x = 0, y = 0, k = 0, kEnd = 1; /* this lane's unit: rays k .. kEnd - 1 of pixel (x, y) */
-    const MixedView* v = p.views;
+    const MixedView* v = kOne ? one : p.views;
     bool exhausted = false, live = false, haveStep = false, waitR = false, waitP = false;
     unsigned reason = 0, bits = 0;
     float pixel[3] = {0.f, 0.f, 0.f};
@@ -486,11 +487,11 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
                         const int within = unit & 31; /* (every view's first unit is a multiple of 32) */
                         if (p.order) {
                             const uint2 slot = __ldg(p.order + (unit >> 5));
-                            v = p.views + (slot.x & 4095u);
+                            if (!kOne) v = p.views + (slot.x & 4095u);
                             plane = v->rayOut ? (int)(slot.x >> 12) : 0;
                             tile = (int)slot.y;
                         } else {
-                            v = p.views + viewOf(p, unit);
+                            if (!kOne) v = p.views + viewOf(p, unit);
                             int local = unit - v->unitBase;
                             plane = v->rayOut ? local / v->pixelUnits : 0;
                             local -= plane * v->pixelUnits;
@@ -583,6 +584,14 @@ __global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) {
     }
     flushTally(t, p.counters);
     flushReasons(n, p.counters);
+}
+
+__global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) { mixedQueue<false>(p, nullptr); }
+
+/* A single view (a frame) as a kernel parameter: its fields are then read from the constant bank where
+ * they are used, not loaded from the view table in global memory at every step. */
+__global__ void __launch_bounds__(256) traceMixedQueueOne(const MixedParams p, const __grid_constant__ MixedView view) {
+    mixedQueue<true>(p, &view);
 }
 
 /* Each pixel of the views with ray planes: its rays' radiance summed in ray order and scaled by
@@ -742,17 +751,18 @@ size_t mixedOrderBytes(int totalTiles, int totalUnits) {
     return kOrderHead + weights + (size_t)(totalUnits / 32) * sizeof(uint2);
 }
 
-int mixedGrid(const TraceLaunch& l, int totalUnits) {
+int mixedGrid(const TraceLaunch& l, int totalUnits, bool one) {
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueue, block, 0);
+    if (one) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueueOne, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueue, block, 0);
     int grid = (perSm > 0 ? perSm : 1) * l.smCount;
     const int needed = (totalUnits + block - 1) / block;
     return grid > needed ? needed : (grid < 1 ? 1 : grid);
 }
 
 cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int viewCount, int totalUnits,
-                             size_t combinePixels, int totalTiles, void* orderScratch) {
+                             size_t combinePixels, int totalTiles, void* orderScratch, const void* hostView) {
     MixedParams p = paramsOf(l, deviceTable, viewCount, totalUnits);
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     if (l.rayCount > 0) {
@@ -772,7 +782,13 @@ cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int 
         placeTiles<<<grid, 128, 0, l.stream>>>(p, totalTiles, weights, classes, cursors, order);
         p.order = order;
     }
-    traceMixedQueue<<<mixedGrid(l, totalUnits), block, 0, l.stream>>>(p);
+    if (hostView && viewCount == 1) {
+        MixedView one;
+        memcpy(&one, hostView, sizeof one);
+        traceMixedQueueOne<<<mixedGrid(l, totalUnits, true), block, 0, l.stream>>>(p, one);
+    } else {
+        traceMixedQueue<<<mixedGrid(l, totalUnits, false), block, 0, l.stream>>>(p);
+    }
     if (combinePixels > 0)
         mixedCombine<<<dim3((unsigned)((combinePixels + 255) / 256), (unsigned)viewCount), 256, 0, l.stream>>>(p.views);
     return cudaGetLastError();

@@ -32,14 +32,15 @@ inline size_t mixedRayPlanes(const TraceLaunch& l, const ArtfCudaHoleFrame& fram
     const size_t rays = l.jitter ? (size_t)l.jitter : (size_t)frame.size[2] * frame.size[2];
     return rays > 1 ? rays : 0;
 }
-/* The persistent grid for a batch of this many units. */
-int mixedGrid(const TraceLaunch& options, int totalUnits);
+/* The persistent grid for a batch of this many units (one: the single-view kernel's). */
+int mixedGrid(const TraceLaunch& options, int totalUnits, bool one);
 /* Launches the trace of a table already on the device (or, with options.rayCount > 0, the ray list of
  * its first view); then, when combinePixels (the largest view's pixel count) is above 0, the sum of
  * the views' ray planes into their frames.  With orderScratch (mixedOrderBytes of device memory) and
  * options.order heavy-first, the tiles are probed and ordered first (two short launches); NULL: the
- * queue runs in pixel order. */
+ * queue runs in pixel order.  hostView: the host's copy of the table's one view (viewCount 1), which the
+ * trace then takes as a kernel parameter; NULL where the table may change under a captured launch. */
 cudaError_t launchMixedTable(const TraceLaunch& options, const void* deviceTable, int viewCount, int totalUnits,
-                             size_t combinePixels, int totalTiles, void* orderScratch);
+                             size_t combinePixels, int totalTiles, void* orderScratch, const void* hostView);
 
 }  // namespace artf

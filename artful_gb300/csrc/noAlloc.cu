@@ -118,7 +118,7 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     cudaError_t e = cudaMemcpyAsync(table, stage, artf::mixedViewBytes() * (size_t)count, cudaMemcpyHostToDevice,
                                     l.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kCounterBytes, l.stream);
-    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0, (int)tiles, nullptr);
+    if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0, (int)tiles, nullptr, nullptr);
     if (e != cudaSuccess) {
         snprintf(line, sizeof line, "allocation-free batch launch: %s", cudaGetErrorString(e));
         return artf::failWith(ARTF_CUDA_ELAUNCH, line);
