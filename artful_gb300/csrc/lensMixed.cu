@@ -131,10 +131,13 @@ __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
     return c;
 }
 
+/* The helpers below take the guards apart from the parameters, so that a kernel built for all of them
+ * passes a constant and its tests fold away. */
+
 /* A ray's start: its constants of motion and first state, in FP64 under the MOTION guard. */
-__device__ __forceinline__ void mixedStart(const MixedParams& p, const MixedView& v, float nx, float ny, float time,
-                                           MixedRay& r) {
-    if (p.guards & ARTF_CUDA_GUARD_MOTION) {
+__device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards, const MixedView& v, float nx,
+                                           float ny, float time, MixedRay& r) {
+    if (guards & ARTF_CUDA_GUARD_MOTION) {
         RayConst<double> cd;
         RayState<double> sd;
         rayStartWith(v.d, v.start64, widen(nx), widen(ny), widen(time), cd, sd);
@@ -163,11 +166,11 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, const MixedView
 }
 
 /* Which sub-steps of this FP32 step must run again in FP64. */
-__device__ __forceinline__ void mixedNeeds(const MixedParams& p, const MixedView& v, const MixedRay& r,
+__device__ __forceinline__ void mixedNeeds(uint32_t guards, const MixedView& v, const MixedRay& r,
                                            const StepOut<float>& o, bool& radial, bool& polar, unsigned& reason) {
-    const bool band = (p.guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > v.uGuard;
-    const bool turnR = (p.guards & ARTF_CUDA_GUARD_RADIAL) && ((r.s.w > 0.f) != (o.next.w > 0.f));
-    polar = (p.guards & ARTF_CUDA_GUARD_POLAR) && ((r.s.v[2] > 0.f) != (o.next.v[2] > 0.f));
+    const bool band = (guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > v.uGuard;
+    const bool turnR = (guards & ARTF_CUDA_GUARD_RADIAL) && ((r.s.w > 0.f) != (o.next.w > 0.f));
+    polar = (guards & ARTF_CUDA_GUARD_POLAR) && ((r.s.v[2] > 0.f) != (o.next.v[2] > 0.f));
     radial = band || turnR;
     reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
 }
@@ -204,10 +207,10 @@ __device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r,
 
 /* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
  * (ARTF_CUDA_END_*) + 1, or 0 when the ray goes on. */
-__device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, const MixedView& v, MixedRay& r,
-                                                 const StepOut<float>& o) {
+__device__ __forceinline__ unsigned mixedAdvance(const MixedParams& p, uint32_t guards, const MixedView& v,
+                                                 MixedRay& r, const StepOut<float>& o) {
     const Frame<float>& f = v.f;
-    const bool compensated = p.guards & ARTF_CUDA_GUARD_PSI;
+    const bool compensated = guards & ARTF_CUDA_GUARD_PSI;
     const float increment = o.next.psi;
     Crossing<float> x;
     if (crossingOf(f, v.rhoScale, r.c, r.s, o, x)) {
@@ -288,14 +291,14 @@ __device__ __forceinline__ void countReason(unsigned reason, Reasons& n) {
 __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const MixedView& v, float nx, float ny,
                                                   float time, float* sum, ArtfCudaRayEnd* end, Tally& t, Reasons& n) {
     MixedRay r;
-    mixedStart(p, v, nx, ny, time, r);
+    mixedStart(p, p.guards, v, nx, ny, time, r);
     unsigned ended = 0;
     while (!ended) {
         StepOut<float> o;
         nystromStep(v.f.a, r.c, r.s, o);
         bool radial, polar;
         unsigned reason;
-        mixedNeeds(p, v, r, o, radial, polar, reason);
+        mixedNeeds(p.guards, v, r, o, radial, polar, reason);
         if (radial || polar) {
             const StepTerms<double> terms = stepTerms(r.step);
             if (radial) radialWide(v, r, terms, (reason & 1u) != 0u, o);
@@ -305,7 +308,7 @@ __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const Mi
             ++r.wide;
             countReason(reason, n);
         }
-        ended = mixedAdvance(p, v, r, o);
+        ended = mixedAdvance(p, p.guards, v, r, o);
     }
     for (int k = 0; k < 3; ++k) sum[k] = sum[k] + r.sum[k];
     return mixedFinish(r, ended, end, t);
@@ -440,8 +443,10 @@ __device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256
 }
 
 /* The warp-scheduled trace (see the file's head).  kOne: a single view, read from `one` (a kernel
- * parameter) rather than from the view table. */
-template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView* one) {
+ * parameter) rather than from the view table.  kAll: every guard on (the default), as a constant. */
+template <bool kOne, bool kAll>
+__device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView* one) {
+    const uint32_t guards = kAll ? (uint32_t)ARTF_CUDA_GUARD_ALL : p.guards;
     /* each lane's ray's step terms in double, formed at its set-up: an FP64 round then loads them
      * where it would multiply them out again (FP64 multiplies are the scarce resource) */
     __shared__ double terms[5][256];
@@ -508,7 +513,7 @@ template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParam
             if (!live && unit >= 0 && k < kEnd) {
                 float nx, ny, moment;
                 samplePosition(v->h, v->jitter, v->seed, x, y, k, &nx, &ny, &moment);
-                mixedStart(p, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
+                mixedStart(p, guards, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
                 const StepTerms<double> t = stepTerms(r.step);
                 terms[0][threadIdx.x] = t.half, terms[1][threadIdx.x] = t.eighth;
                 terms[2][threadIdx.x] = t.halfSquare, terms[3][threadIdx.x] = t.sixthSquare;
@@ -549,7 +554,7 @@ template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParam
         for (int j = 0; j < kInnerSteps; ++j) {
             if (haveStep && !waitR && !waitP) {
                 haveStep = false;
-                const unsigned ended = mixedAdvance(p, *v, r, o);
+                const unsigned ended = mixedAdvance(p, guards, *v, r, o);
                 if (ended) {
                     const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
                     ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)v->rays + (size_t)k : nullptr;
@@ -573,7 +578,7 @@ template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParam
             }
             if (live && !haveStep) {
                 nystromStep(v->f.a, r.c, r.s, o);
-                mixedNeeds(p, *v, r, o, waitR, waitP, reason);
+                mixedNeeds(guards, *v, r, o, waitR, waitP, reason);
                 haveStep = true;
                 if (waitR || waitP) {
                     ++r.wide;
@@ -586,12 +591,20 @@ template <bool kOne> __device__ __forceinline__ void mixedQueue(const MixedParam
     flushReasons(n, p.counters);
 }
 
-__global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) { mixedQueue<false>(p, nullptr); }
+/* The views from the table (a batch).  The kernels come in pairs: the guards chosen at run time, and all
+ * of them as constants, which every trace with all guards runs (frames, bands and batches alike, so that
+ * their bits agree): its dead branches fold away and its code is smaller. */
+__global__ void __launch_bounds__(256) traceMixedQueue(const MixedParams p) { mixedQueue<false, false>(p, nullptr); }
+__global__ void __launch_bounds__(256) traceMixedQueueAll(const MixedParams p) { mixedQueue<false, true>(p, nullptr); }
 
 /* A single view (a frame) as a kernel parameter: its fields are then read from the constant bank where
  * they are used, not loaded from the view table in global memory at every step. */
 __global__ void __launch_bounds__(256) traceMixedQueueOne(const MixedParams p, const __grid_constant__ MixedView view) {
-    mixedQueue<true>(p, &view);
+    mixedQueue<true, false>(p, &view);
+}
+__global__ void __launch_bounds__(256) traceMixedQueueOneAll(const MixedParams p,
+                                                             const __grid_constant__ MixedView view) {
+    mixedQueue<true, true>(p, &view);
 }
 
 /* Each pixel of the views with ray planes: its rays' radiance summed in ray order and scaled by
@@ -751,11 +764,10 @@ size_t mixedOrderBytes(int totalTiles, int totalUnits) {
     return kOrderHead + weights + (size_t)(totalUnits / 32) * sizeof(uint2);
 }
 
-int mixedGrid(const TraceLaunch& l, int totalUnits, bool one) {
+int mixedGrid(const TraceLaunch& l, int totalUnits, const void* kernel) {
     const int block = l.blockSize > 0 ? l.blockSize : 128;
     int perSm = 0;
-    if (one) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueueOne, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, traceMixedQueue, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, block, 0);
     int grid = (perSm > 0 ? perSm : 1) * l.smCount;
     const int needed = (totalUnits + block - 1) / block;
     return grid > needed ? needed : (grid < 1 ? 1 : grid);
@@ -782,12 +794,19 @@ cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int 
         placeTiles<<<grid, 128, 0, l.stream>>>(p, totalTiles, weights, classes, cursors, order);
         p.order = order;
     }
+    const bool all = p.guards == ARTF_CUDA_GUARD_ALL;
     if (hostView && viewCount == 1) {
         MixedView one;
         memcpy(&one, hostView, sizeof one);
-        traceMixedQueueOne<<<mixedGrid(l, totalUnits, true), block, 0, l.stream>>>(p, one);
+        const void* kernel = all ? (const void*)traceMixedQueueOneAll : (const void*)traceMixedQueueOne;
+        const int grid = mixedGrid(l, totalUnits, kernel);
+        if (all) traceMixedQueueOneAll<<<grid, block, 0, l.stream>>>(p, one);
+        else traceMixedQueueOne<<<grid, block, 0, l.stream>>>(p, one);
     } else {
-        traceMixedQueue<<<mixedGrid(l, totalUnits, false), block, 0, l.stream>>>(p);
+        const void* kernel = all ? (const void*)traceMixedQueueAll : (const void*)traceMixedQueue;
+        const int grid = mixedGrid(l, totalUnits, kernel);
+        if (all) traceMixedQueueAll<<<grid, block, 0, l.stream>>>(p);
+        else traceMixedQueue<<<grid, block, 0, l.stream>>>(p);
     }
     if (combinePixels > 0)
         mixedCombine<<<dim3((unsigned)((combinePixels + 255) / 256), (unsigned)viewCount), 256, 0, l.stream>>>(p.views);

@@ -32,8 +32,8 @@ inline size_t mixedRayPlanes(const TraceLaunch& l, const ArtfCudaHoleFrame& fram
     const size_t rays = l.jitter ? (size_t)l.jitter : (size_t)frame.size[2] * frame.size[2];
     return rays > 1 ? rays : 0;
 }
-/* The persistent grid for a batch of this many units (one: the single-view kernel's). */
-int mixedGrid(const TraceLaunch& options, int totalUnits, bool one);
+/* The persistent grid of the given queue kernel for a batch of this many units. */
+int mixedGrid(const TraceLaunch& options, int totalUnits, const void* kernel);
 /* Launches the trace of a table already on the device (or, with options.rayCount > 0, the ray list of
  * its first view); then, when combinePixels (the largest view's pixel count) is above 0, the sum of
  * the views' ray planes into their frames.  With orderScratch (mixedOrderBytes of device memory) and
