@@ -815,8 +815,9 @@ __device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py,
  * lanes stay busy together), a block four tiles of one view (blockIdx.y).  Each warp writes its tile's
  * sums to the tile's own slot and leaves: no warp waits for another once the view is in shared memory.
  * (A persistent grid taking tiles from a device counter measured slower: its warps hold more ray state
- * resident at once.) */
-__global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L) {
+ * resident at once.)  kK: the checkpoint interval as a constant (the default, 32: the ring's index and
+ * the checkpoint's are then a mask and a shift, not divisions), or 0 to read it from L. */
+template <int kK> __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L) {
     __shared__ AdjointView v;
     {
         const int4* src = reinterpret_cast<const int4*>(L.views + blockIdx.y);
@@ -831,7 +832,7 @@ __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L)
     const int px = (local % L.tilesX) * 8 + (lane & 7), py = (local / L.tilesX) * 4 + (lane >> 3);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     Tally tally;
-    if (px < v.f.width && py < v.f.height) adjointRay(v, px, py, L.K, acc, tally);
+    if (px < v.f.width && py < v.f.height) adjointRay(v, px, py, kK ? kK : L.K, acc, tally);
     flushTally(tally, L.counters);
     const size_t tile = (size_t)blockIdx.y * L.tilesPerView + local;
 #pragma unroll
@@ -982,7 +983,8 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
         L.order = order;
     }
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
-    adjointPixels<<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
+    if (K == 32) adjointPixels<32><<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
+    else adjointPixels<0><<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
     adjointSums<<<count, 256, 0, stream>>>(partials, L.tilesPerView, results);
     return cudaGetLastError();
 }
