@@ -167,3 +167,31 @@ def test_heavy_first_gives_the_same_bits(lib, ctx, jitter):
         assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32)), i
         assert np.array_equal(ea, eb), i
     assert lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(_opts(order=2)), None) == -1  # ARTF_CUDA_EINVAL
+
+
+@pytest.mark.parametrize("guards", [0, capi.GUARD_MOTION | capi.GUARD_RADIAL | capi.GUARD_PSI])
+def test_every_queue_kernel_gives_a_view_the_same_bits(lib, ctx, guards):
+    """A frame runs the single-view queue kernel (its view a kernel parameter) and a graph of that one
+    view the view table's; each has a form with the guards chosen at run time and one with all of them as
+    constants.  Both pairs give the view the same bytes, four jittered rays a pixel (ray planes)."""
+    import torch
+    views, keep = _views(lib, count=1, scale=0.5, rays=4)
+    scene, m, fluid, hdr, ends = keep[0]
+    opts = _opts(jitter=4, seed=7, guards=guards)
+    capi.check(lib.artfCudaHoleTrace(ctx, C.byref(views[0].frame), C.byref(views[0].frame64), m.data_ptr(),
+                                     fluid.data_ptr(), C.byref(opts), hdr.data_ptr(), ends.data_ptr(),
+                                     C.byref(capi.TraceStats())))
+    torch.cuda.synchronize()
+    alone, alone_ends = hdr.cpu().numpy().copy(), ends.cpu().numpy().copy()
+    assert (alone[..., :3] > 0).any()
+    hdr.zero_()
+    ends.zero_()
+    graph = C.c_void_p()
+    capi.check(lib.artfCudaBatchGraphCreate(ctx, views, 1, C.byref(opts), C.byref(graph)))
+    try:
+        capi.check(lib.artfCudaBatchGraphLaunch(graph, C.byref(capi.TraceStats())))
+        torch.cuda.synchronize()
+        assert np.array_equal(hdr.cpu().numpy().view(np.uint32), alone.view(np.uint32))
+        assert np.array_equal(ends.cpu().numpy(), alone_ends)
+    finally:
+        lib.artfCudaBatchGraphDestroy(graph)
