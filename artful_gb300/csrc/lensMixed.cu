@@ -432,7 +432,8 @@ __global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int total
 }
 
 /* FP32 steps a lane takes between two of the warp's votes on refills and FP64 rounds (measured at
- * 1080p x 4: 3 steps 2.64 ms, 4 steps 2.62, 6 steps 2.60; the 64-view batch alike). */
+ * 1080p x 4: 3 steps 2.64 ms, 4 steps 2.62, 6 steps 2.60, 8 steps 2.60, 10 steps 2.62; the 64-view batch
+ * alike). */
 constexpr int kInnerSteps = 6;
 
 /* This lane's step terms, from the block's table. */
