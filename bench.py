@@ -441,6 +441,15 @@ def main():
     peak = fp32_peak.value / 1e12
     achieved64 = s_mixed.flops64 / (ms_mixed * 1e-3) / 1e12
     peak64 = fp64_peak.value / 1e12
+    # HBM beside it, to show it is not the bound: the trace's DRAM bytes a frame against the measured copy
+    hbm = {"achieved": TRACE_TRAFFIC_BYTES / (ms_mixed * 1e-3) / 1e9, "unit": "GB/s"}
+    peaks_path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            hbm.update(peak=float(json.load(fh)["hbm_gbs"]), peak_source="MEASURED_PEAKS.json, of measured")
+    else:
+        hbm.update(peak=6800.0, peak_source="6.8 TB/s, of fallback")
+    hbm["frac"] = hbm["achieved"] / hbm["peak"]
     # the other traces against their own pipe: FP32 (exact, fast) and FP64 (plain), of the measured peaks
     for name, pipe_peak in (("fp32_exact", peak), ("fp32_fast", peak), ("fp64", peak64)):
         entry = side[name]
@@ -494,6 +503,7 @@ def main():
                      "flops64_per_frame": s_mixed.flops64,
                      "fp32": {"achieved": achieved, "peak": peak, "frac": achieved / peak,
                               "flops_per_frame": s_mixed.flops},
+                     "hbm": hbm,
                      "time": "the whole timed step (probe, order, trace, combine)"},
         "e2e": {"value": world * geodesics / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": (map_.nbytes + fluid.nbytes), "d2h_bytes_per_step": h * w * 16},
