@@ -620,6 +620,24 @@ ARTF_HD uint32_t mix32(uint32_t x) {
     return x;
 }
 
+/* A float product rounded on its own, never fused with the sum it feeds: the sample positions below are
+ * the reference's to the bit in every unit, including those built with contraction and fast division. */
+ARTF_HD float mulRn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+/* A correctly rounded float quotient, whatever the unit's division flags. */
+ARTF_HD float divRn(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+
 /* Ray k of pixel (x, y): its image position and its moment within the shutter.  jitter 0: the
  * reference's stratified side x side samples, with its float arithmetic (lens.inc:365-371: the
  * eight-pixel group's base column plus the lane); jitter n: n uniform offsets hashed from the seed. */
@@ -628,18 +646,18 @@ ARTF_HD void samplePosition(const ArtfCudaHoleFrame& h, int jitter, uint32_t see
     if (!jitter) {
         const int32_t side = (int32_t)h.size[2];
         const int32_t sy = k / side, sx = k - sy * side;
-        const float dx = ((float)sx + .5f) / (float)side, dy = ((float)sy + .5f) / (float)side;
+        const float dx = divRn((float)sx + .5f, (float)side), dy = divRn((float)sy + .5f, (float)side);
         const int32_t group = x & ~7, lane = x & 7;
-        *nx = ((float)lane + ((float)group + dx)) * h.image[1] - 1.f;
-        *ny = 1.f - ((float)y + dy) * h.image[2];
-        *moment = ((float)((sy * side + sx) * 5 % (side * side)) + .5f) * h.image[3] - .5f;
+        *nx = mulRn((float)lane + ((float)group + dx), h.image[1]) - 1.f;
+        *ny = 1.f - mulRn((float)y + dy, h.image[2]);
+        *moment = mulRn((float)((sy * side + sx) * 5 % (side * side)) + .5f, h.image[3]) - .5f;
     } else {
         const uint32_t base = mix32(mix32(seed ^ 0xA511E9B3u) ^ ((uint32_t)y * h.size[0] + (uint32_t)x));
-        const float dx = (float)(mix32(base + 2u * (uint32_t)k) >> 8) * (1.f / 16777216.f);
-        const float dy = (float)(mix32(base + 2u * (uint32_t)k + 1u) >> 8) * (1.f / 16777216.f);
-        *nx = ((float)x + dx) * h.image[1] - 1.f;
-        *ny = 1.f - ((float)y + dy) * h.image[2];
-        *moment = ((float)(k * 5 % jitter) + .5f) / (float)jitter - .5f;
+        const float dx = mulRn((float)(mix32(base + 2u * (uint32_t)k) >> 8), 1.f / 16777216.f);
+        const float dy = mulRn((float)(mix32(base + 2u * (uint32_t)k + 1u) >> 8), 1.f / 16777216.f);
+        *nx = mulRn((float)x + dx, h.image[1]) - 1.f;
+        *ny = 1.f - mulRn((float)y + dy, h.image[2]);
+        *moment = divRn((float)(k * 5 % jitter) + .5f, (float)jitter) - .5f;
     }
 }
 

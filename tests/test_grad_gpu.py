@@ -176,7 +176,11 @@ def test_adjoint_workload_per_pixel(lib, ctx, torch, scene):
     assert same.mean() >= 0.995
     ref = np.stack([(2.0 * (value - target) * tan[..., 1 + q]).sum(-1) / value.size for q in range(5)], -1)
     got = shares.cpu().numpy()[0]
-    np.testing.assert_allclose(got.reshape(-1, 5).sum(0), grad[0], rtol=1e-4, atol=1e-9)
+    # the shares add up to the gradient, to the rounding of the float sums that formed it (a warp adds its
+    # pixels' float shares before the tiles are added in double): bounded by the shares' magnitudes, since
+    # a component's total may be far smaller than its parts
+    flat = got.reshape(-1, 5).astype(np.float64)
+    assert np.all(np.abs(flat.sum(0) - grad[0]) <= 1e-5 * np.abs(flat).sum(0) + 1e-12), (flat.sum(0), grad[0])
     for q in range(5):
         floor = 1e-2 * np.abs(ref[..., q]).max()
         carry = same & (np.maximum(np.abs(ref[..., q]), np.abs(got[..., q])) > floor)
