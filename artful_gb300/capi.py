@@ -226,7 +226,7 @@ class HoleInputs(C.Structure):
 
 
 class RendererVtbl(C.Structure):
-    """The eight entries of Artful's ArtfRendererVtbl (src/render/rendererInternal.h:146-155)."""
+    """The eight entries of Artful's ArtfRendererVtbl (src/render/rendererInternal.h:7-16)."""
     _fields_ = [("description", C.CFUNCTYPE(C.c_char_p, C.c_void_p)),
                 ("resize", C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int)),
                 ("setOverlay", C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)),
@@ -238,7 +238,7 @@ class RendererVtbl(C.Structure):
 
 
 class RendererHead(C.Structure):
-    """struct ArtfRenderer's head (src/render/rendererInternal.h:157-163)."""
+    """struct ArtfRenderer's head (src/render/rendererInternal.h:18-27)."""
     _fields_ = [("vt", C.POINTER(RendererVtbl)), ("backend", C.c_int), ("trialFrame", C.c_int),
                 ("trialMs", C.c_double * 2)]
 

@@ -1,6 +1,6 @@
 /* artful_cuda — the GB300 hole tracer as an Artful renderer backend (C11), and the library's own
  * minimal hole scene.  The backend fills the eight-entry table every Artful renderer has
- * (src/render/rendererInternal.h:146-163) and draws through the C ABI: the trace, its bloom and tone
+ * (src/render/rendererInternal.h:7-27) and draws through the C ABI: the trace, its bloom and tone
  * map on the GPU, and the frame read back for readPixels.  Its rules are the reference's:
  *   - draw returns false when the device is lost; the renderer must then be freed, and the scene
  *     survives for a new one (include/artful/renderer.h:107-109);

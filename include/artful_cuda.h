@@ -160,7 +160,7 @@ void artfCudaDestroy(ArtfCuda* ctx);
 int artfCudaSetMap(ArtfCuda* ctx, const float* hostMap, uint64_t version);
 int artfCudaSetFluid(ArtfCuda* ctx, const float* hostFluid, uint64_t version);
 /* Fault injection on the host, for tests of device loss (the reference's artfVulkanSubmitsLeft,
- * src/render/rendererInternal.h:166-167): after `launches` more launches the context reports
+ * src/render/rendererInternal.h:29-30): after `launches` more launches the context reports
  * ARTF_CUDA_ELOST, as after a device loss, without the GPU being touched.  -1 turns it off. */
 int artfCudaFailAfter(ArtfCuda* ctx, int launches);
 /* The device copies, for callers that launch on their own buffers. */

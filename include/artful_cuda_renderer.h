@@ -1,15 +1,15 @@
 /* artful_cuda — the GB300 hole tracer as an Artful renderer backend, beside Vulkan and software.
  *
  * The renderer is an object that begins with a table of eight functions, as every Artful backend does
- * (src/render/rendererInternal.h:146-163: ArtfRendererVtbl and struct ArtfRenderer): Artful's public
+ * (src/render/rendererInternal.h:7-27: ArtfRendererVtbl and struct ArtfRenderer): Artful's public
  * calls (artfRendererDraw, ReadPixels, Stats, ...) dispatch through it unchanged.  This backend draws
  * the black hole only: the trace on the GPU, then its bloom and tone map, to BGRA.
  *
  * A backend reads the scene.  In Artful's own tree the scene is the internal ArtfScene; this library
  * cannot include it, so the renderer reads a scene through an ArtfCudaSceneReader, a function that
  * fills ArtfCudaHoleInputs from whatever the scene pointer points at.  The reader for Artful's scene is
- * a few lines in the backend file a maintainer adds; the reader for ArtfCudaScene,
- * this library's own minimal hole scene, is built in. */
+ * a few lines in the backend file a maintainer adds to Artful's tree (src/cuda/, beside its other
+ * backends); the reader for ArtfCudaScene, this library's own minimal hole scene, is built in. */
 #ifndef ARTFUL_CUDA_RENDERER_H
 #define ARTFUL_CUDA_RENDERER_H
 
@@ -65,7 +65,7 @@ typedef struct ArtfCudaFrameStats {
 
 typedef struct ArtfCudaRenderer ArtfCudaRenderer;
 
-/* The table every backend fills (src/render/rendererInternal.h:146-155). */
+/* The table every backend fills (src/render/rendererInternal.h:7-16). */
 typedef struct ArtfCudaRendererVtbl {
     const char* (*description)(const ArtfCudaRenderer* r);
     void (*resize)(ArtfCudaRenderer* r, int width, int height);
@@ -77,7 +77,7 @@ typedef struct ArtfCudaRendererVtbl {
     void (*destroy)(ArtfCudaRenderer* r);
 } ArtfCudaRendererVtbl;
 
-/* The head every renderer starts with (src/render/rendererInternal.h:157-163). */
+/* The head every renderer starts with (src/render/rendererInternal.h:18-27). */
 struct ArtfCudaRenderer {
     const ArtfCudaRendererVtbl* vt;
     int backend;

@@ -4,7 +4,9 @@
 # x86-64 or aarch64 gcc; the reference's own CMake build is not used.
 #
 #   make -f oracle/ref.mk REF=/path/to/artful -j8
-REF ?= /root/reference
+ifeq ($(REF),)
+  $(error REF must name the reference checkout)
+endif
 HERE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT := $(HERE)_ref
 CC ?= gcc

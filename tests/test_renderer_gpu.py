@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 class Backend:
-    """A renderer made by artfCudaNew, called only through its table (rendererInternal.h:146-155)."""
+    """A renderer made by artfCudaNew, called only through its table (rendererInternal.h:7-16)."""
 
     def __init__(self, lib, width, height):
         self.lib = lib
