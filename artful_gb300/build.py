@@ -38,7 +38,7 @@ UNITS = {
     "fluid.cu": EXACT,
     "disc.cu": EXACT,
 }
-C_UNITS = ["holeHost.c", "renderer.c"]
+C_UNITS = ["holeHost.c", "synthScene.c", "renderer.c"]
 CFLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wextra", "-I" + INCLUDE]
 
 

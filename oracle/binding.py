@@ -24,6 +24,34 @@ class OracleEnd(C.Structure):
                 ("fp64Steps", C.c_uint16), ("reserved", C.c_uint16)]
 
 
+FRAME_FIELDS = ("er", "etheta", "ephi", "right", "up", "forward", "metric", "place", "spin", "flow", "boost", "disc",
+                "look", "image")
+
+
+class Frame64(C.Structure):
+    """The frame's fields in double (oracle.h OracleFrame64)."""
+    _fields_ = [(n, C.c_double * 4) for n in FRAME_FIELDS]
+
+
+def widened(frame, shift=(0.0, 0.0)) -> Frame64:
+    """The FP32 frame's fields in double, the same values: what an FP64 trace of the reference's own rays
+    starts from.  shift moves every ray's image position by (dx, dy) (forward += dx right + dy up)."""
+    w = Frame64()
+    for n in FRAME_FIELDS:
+        src, dst = getattr(frame, n), getattr(w, n)
+        for k in range(4):
+            dst[k] = float(src[k])
+    for k in range(3):
+        w.forward[k] += shift[0] * w.right[k] + shift[1] * w.up[k]
+    return w
+
+
+class SynthDesc(C.Structure):
+    """The synthetic scene's description (include/artful_cuda.h ArtfCudaSynthDesc)."""
+    _fields_ = [("seed", C.c_uint64), ("inner", C.c_float), ("outer", C.c_float), ("spin", C.c_float),
+                ("emissivity", C.c_float), ("stars", C.c_int)]
+
+
 class OracleOptions(C.Structure):
     _fields_ = [("stepScale", C.c_float)]
 
@@ -66,6 +94,8 @@ def oracle() -> C.CDLL:
         lib.oracleFluidFree.argtypes = [vp]
         lib.oraclePaintDisc.argtypes = [vp]
         lib.oracleSetRings.argtypes = [vp, C.c_float, C.c_float, C.c_float]
+        lib.artfCudaSynthMap.argtypes = [C.POINTER(SynthDesc), vp]
+        lib.artfCudaSynthMap.restype = C.c_int
         _oracle = lib
     return _oracle
 
@@ -131,6 +161,16 @@ def render64(frame, frame64, map_, fluid, jitter=0, seed=0, threads=0, rows=None
     oracle().oracleRender64(C.byref(frame), C.byref(frame64), _ptr(map_), _ptr(fluid),
                             C.byref(OracleOptions(step_scale)), jitter, seed, threads, y0, y1, _ptr(hdr), _ptr(e))
     return (hdr, e) if ends else hdr
+
+
+def synth_map(inner: float, outer: float, spin: float, seed: int, emissivity: float, stars: int = 2000):
+    """The benchmark's synthetic map for a disc (the library's generator source, built into the oracle's
+    library): what the CPU arm reads, with no CUDA library loaded."""
+    m = np.zeros(MAP_FLOATS, np.float32)
+    status = oracle().artfCudaSynthMap(C.byref(SynthDesc(seed, inner, outer, spin, emissivity, stars)), m.ctypes.data)
+    if status != 0:
+        raise ValueError("bad synthetic scene")
+    return m
 
 
 def post(frame, hdr):

@@ -60,6 +60,18 @@ def test_synthetic_map_is_reproducible(lib, golden, name):
     assert hashlib.sha256(m.tobytes()).hexdigest() == meta["views"][name]["map_sha256"]
 
 
+@pytest.mark.parametrize("name", list(scenes.golden_scenes()))
+def test_synthetic_map_from_the_oracle_library(golden, name):
+    """The CPU arm reads its map from the oracle's library (the same generator source): the same bytes,
+    made from the reference's clamped description alone."""
+    from oracle import binding
+    meta, _ = golden
+    scene = scenes.golden_scenes()[name]
+    clamped = capi.BlackHoleDesc.from_buffer_copy(bytes.fromhex(meta["views"][name]["clamped_hex"]))
+    m = binding.synth_map(clamped.discInner, clamped.discOuter, clamped.spin, scene.seed, scene.emissivity)
+    assert hashlib.sha256(m.tobytes()).hexdigest() == meta["views"][name]["map_sha256"]
+
+
 def test_synthetic_map_contents(lib):
     scene = scenes.config1()
     _, _, d = scenes.frame(scene)

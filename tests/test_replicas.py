@@ -64,3 +64,18 @@ def test_reference_arm_under_torchrun(oracle_lib, lib):
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_loads_no_cuda_library(oracle_lib):
+    """The reference arm's inputs and trace come from the oracle's library alone: after a run, the process
+    has mapped liboracle.so and not the CUDA library (nor torch's CUDA runtime)."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0']; "
+            "runpy.run_path('bench.py', run_name='__main__'); maps = open('/proc/self/maps').read(); "
+            "print('MAPS', 'libartful_cuda' in maps, 'liboracle' in maps, 'libcudart' in maps)")
+    run = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stderr[-2000:]
+    maps = [x for x in run.stdout.splitlines() if x.startswith("MAPS")]
+    assert maps == ["MAPS False True False"], run.stdout[-2000:]
+    line = json.loads([x for x in run.stdout.splitlines() if x.startswith("{")][0])
+    assert line["config"]["workload"].startswith("kerr-hole 1920x1080")
+    assert "whole 1920x1080 frame" in line["cpu_baseline"]["sample"]
