@@ -1,6 +1,7 @@
 /* artful_cuda — the C ABI's device side: contexts, uploads, the trace dispatch, batches of views, their
  * CUDA graphs and the autotuner.  Every entry point checks its arguments and every CUDA call, and
  * reports failure by status, never by abort. */
+#include "nvtxRange.h"
 #include "artful_cuda.h"
 #include "lensFlops.h"
 #include "lensLaunch.h"
@@ -476,6 +477,7 @@ extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* fra
                                      const float* map, const float* fluid, int precision, float stepScale, int n,
                                      const float* nx, const float* ny, const float* time, float* rgb,
                                      ArtfCudaRayEnd* ends, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleTraceRays");
     int status = enter(ctx);
     if (status) return status;
     ArtfCudaTraceOptions o;
@@ -503,6 +505,7 @@ extern "C" int artfCudaHoleTraceRays(ArtfCuda* ctx, const ArtfCudaHoleFrame* fra
 extern "C" int artfCudaHoleTrace(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
                                  const float* map, const float* fluid, const ArtfCudaTraceOptions* options, float* hdr,
                                  ArtfCudaRayEnd* ends, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleTrace");
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
@@ -524,6 +527,7 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
                                   const float* hostMap, uint64_t mapVersion, const float* hostFluid,
                                   uint64_t fluidVersion, const ArtfCudaTraceOptions* options, float* hostHdr,
                                   ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleRender");
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
@@ -560,6 +564,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
                                 const float* hostMap, uint64_t mapVersion, const float* hostFluid,
                                 uint64_t fluidVersion, const ArtfCudaTraceOptions* options, float* hostHdr,
                                 uint32_t* hostBgra, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleDraw");
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
@@ -601,6 +606,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
 extern "C" int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* params, const ArtfCudaHoleFrame* frame,
                                     const ArtfCudaHoleFrame64* frame64, const double* jacobian, const float* map,
                                     const float* fluid, double* out) {
+    artf::Range range("artfCudaHoleTangents");
     int status = enter(ctx);
     if (status) return status;
     if (!params || !frame || !frame64 || !jacobian || !out) return fail(ARTF_CUDA_EINVAL, "a NULL argument");
@@ -652,6 +658,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
                                    const float* map, const float* fluid, const float* targets, int checkpointEvery,
                                    float* hdr, float* pixelGrads, ArtfCudaAdjointResult* results,
                                    ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleAdjoint");
     int status = enter(ctx);
     if (status) return status;
     if (!params || !targets || !results) return fail(ARTF_CUDA_EINVAL, "params, targets and results are required");
@@ -754,6 +761,7 @@ static int checkBatch(const ArtfCudaView* views, int count, const ArtfCudaTraceO
 
 extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int count,
                                  const ArtfCudaTraceOptions* options, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleBatch");
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkBatch(views, count, options))) return status;
@@ -808,6 +816,7 @@ extern "C" void artfCudaBatchGraphDestroy(ArtfCudaGraph* g) {
 
 extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views, int count,
                                         const ArtfCudaTraceOptions* options, ArtfCudaGraph** out) {
+    artf::Range range("artfCudaBatchGraphCreate");
     int status = enter(ctx);
     if (status) return status;
     if (!out) return fail(ARTF_CUDA_EINVAL, "out is NULL");
@@ -881,6 +890,7 @@ extern "C" int artfCudaBatchGraphUpdate(ArtfCudaGraph* g, const ArtfCudaView* vi
 }
 
 extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaBatchGraphLaunch");
     if (!g) return fail(ARTF_CUDA_EINVAL, "no graph");
     ArtfCuda* ctx = g->ctx;
     int status = enter(ctx);
@@ -922,6 +932,7 @@ static int timeBatch(ArtfCuda* ctx, const artf::TraceLaunch& l, int count, int u
 
 extern "C" int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int count,
                                 const ArtfCudaTraceOptions* options, ArtfCudaTuning* result) {
+    artf::Range range("artfCudaAutotune");
     int status = enter(ctx);
     if (status) return status;
     if (!result) return fail(ARTF_CUDA_EINVAL, "result is NULL");

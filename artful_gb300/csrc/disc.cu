@@ -10,6 +10,7 @@
  * fixed tree order: the sum is of floats of moderate range, its double rounding leaves the float scale
  * derived from it unchanged, and the test holds the whole map to the reference's bytes.  The colour and
  * ring tables (4 K floats) come from the host set-up (holeHost.c), as the reference computes them. */
+#include "nvtxRange.h"
 #include "artful_cuda.h"
 
 #include <cuda_runtime.h>
@@ -164,6 +165,7 @@ __global__ void __launch_bounds__(256) paintSky(float* __restrict__ map) {
 }  // namespace
 
 extern "C" int artfCudaPaintDisc(ArtfCuda* ctx, float* map, float inner, float outer, float spin) {
+    artf::Range range("artfCudaPaintDisc");
     cudaStream_t stream = nullptr;
     if (int s = artf::contextStream(ctx, &stream)) return s;
     if (!(inner > 0.f) || !(outer > inner) || !(fabsf(spin) <= 1.f))

@@ -17,6 +17,7 @@
  *
  * Work layout: 7 fields of 256 x 1024 floats (7 MB, L2-resident), one allocation; per step five launches
  * on the context's stream (stir, velocities, densities, shift, balance), and the field after the last. */
+#include "nvtxRange.h"
 #include "artful_cuda.h"
 
 #include <cuda_runtime.h>
@@ -364,6 +365,7 @@ extern "C" void artfCudaFluidFree(ArtfCudaFluid* f) {
 
 extern "C" int artfCudaFluidNew(ArtfCuda* ctx, float inner, float outer, float spin, double time,
                                 ArtfCudaFluid** out) {
+    artf::Range range("artfCudaFluidNew");
     if (!out) return artf::failWith(ARTF_CUDA_EINVAL, "out is NULL");
     *out = nullptr;
     if (!(inner > 0.f) || !(outer > inner) || !(fabsf(spin) <= 1.f) || !isfinite(time))
@@ -420,6 +422,7 @@ extern "C" int artfCudaFluidNew(ArtfCuda* ctx, float inner, float outer, float s
 }
 
 extern "C" int artfCudaFluidAdvance(ArtfCudaFluid* f, double time, int* stepped) {
+    artf::Range range("artfCudaFluidAdvance");
     if (stepped) *stepped = 0;
     if (!f || !isfinite(time)) return artf::failWith(ARTF_CUDA_EINVAL, "no fluid, or a time that is not finite");
     cudaStream_t stream = nullptr;
@@ -434,6 +437,7 @@ extern "C" int artfCudaFluidAdvance(ArtfCudaFluid* f, double time, int* stepped)
 }
 
 extern "C" int artfCudaFluidStep(ArtfCudaFluid* f, int64_t steps, double time) {
+    artf::Range range("artfCudaFluidStep");
     if (!f || steps < 0 || !isfinite(time)) return artf::failWith(ARTF_CUDA_EINVAL, "fluid step: no fluid, or bad steps or time");
     cudaStream_t stream = nullptr;
     if (int s = artf::contextStream(f->ctx, &stream)) return s;

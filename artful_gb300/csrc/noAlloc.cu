@@ -13,6 +13,7 @@
  * any stream capture.  All calls share the array and it keeps the last call's contents; each call
  * writes the table and clears the counters before its launch.  Calls whose work overlaps on the GPU
  * (on different streams, or from different threads) race on the array: order them on one stream. */
+#include "nvtxRange.h"
 #include "artful_cuda.h"
 #include "lensLaunch.h"
 #include "lensMixed.h"
@@ -62,6 +63,7 @@ int scratchAddress(int device, unsigned char** out) {
 
 extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options,
                                         void* stream, ArtfCudaTraceStats* stats) {
+    artf::Range range("artfCudaHoleBatchNoAlloc");
     char line[200];
     if (!views || !options) return artf::failWith(ARTF_CUDA_EINVAL, "views or options is NULL");
     if (count < 1 || count > ARTF_CUDA_NOALLOC_MAX_VIEWS) {

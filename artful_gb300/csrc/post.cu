@@ -10,6 +10,7 @@
  * before; then each level, from the top down, adds four taps of the one above, times 0.85.  The tone
  * map reads level 0 between its texels, turns its glow toward grey (0.9), adds it times bloom * 0.15,
  * scales by the exposure, applies Narkowicz's ACES fit and a square root, and dithers by a hash. */
+#include "nvtxRange.h"
 #include "artful_cuda.h"
 
 #include <cuda_runtime.h>
@@ -133,6 +134,7 @@ __global__ void toneMap(const float4* hdr, int width, int height, Planes bloom, 
 /* The pyramid and tone map of one frame; bloom: three planes of the frame's bloom pixel count. */
 extern "C" int artfCudaPostLaunch(const ArtfCudaHoleFrame* frame, const float* hdr, float* const bloomPlanes[3],
                                   uint32_t* bgra, void* stream) {
+    artf::Range range("artfCudaPostLaunch");
     if (!frame || !hdr || !bloomPlanes || !bgra) return ARTF_CUDA_EINVAL;
     const int width = (int)frame->size[0], height = (int)frame->size[1], levels = (int)frame->size[3];
     if (width < 1 || height < 1 || levels < 1 || levels > ARTF_CUDA_BLOOM_LEVELS) return ARTF_CUDA_EINVAL;
