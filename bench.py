@@ -16,7 +16,8 @@ differences.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--fd-fits F]
 
 --impl reference times the reference's CPU path on this host's cores: the oracle port (the reference's
-own sources are not on this machine), with all host threads, on a bounded sample of the same frame.
+lensTrace in scalar C, bit for bit; its own sources are not on this machine), with all host threads, on
+the same whole frame every step, its inputs made without the CUDA library.
 """
 from __future__ import annotations
 
@@ -34,6 +35,8 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+from artful_gb300.endpoint import END_DTYPE, endpoint_error  # noqa: E402  (numpy only: loads no library)
 
 METRIC = "geodesics/s @1080p: mixed-prec vs FP64 GPU at ≤1e-4 endpoint err; adj/fwd time"
 UNIT = "geodesics/s"
@@ -74,7 +77,6 @@ def sweep(args):
     FP64 at the same step and at half step."""
     import torch
     from artful_gb300 import capi, scenes
-    from oracle.binding import END_DTYPE
     lib = capi.load()
     ctx = C.c_void_p()
     capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
@@ -90,12 +92,12 @@ def sweep(args):
 
     def run(opts, with_ends=False, steps=0):
         s = capi.TraceStats()
-        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts),
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(opts),
                                          hdr.data_ptr(), ends.data_ptr() if with_ends else None, C.byref(s)))
         times = []
         for _ in range(steps):
             t = capi.TraceStats()
-            capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts),
+            capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(opts),
                                              hdr.data_ptr(), None, C.byref(t)))
             times.append(t.ms)
         e = np.frombuffer(ends.cpu().numpy().tobytes(), END_DTYPE).copy() if with_ends else None
@@ -176,7 +178,7 @@ def profile_case(args):
                           1 if args.persistent else 0, args.guards)
     for _ in range(2):
         s = capi.TraceStats()
-        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(o),
                                          hdr.data_ptr(), None, C.byref(s)))
     print(json.dumps({"profile": args.profile, "width": scene.width, "height": scene.height, "ms": s.ms,
                       "rays": s.rays, "steps": s.steps, "fp64Steps": s.fp64Steps, "flops": s.flops}))
@@ -259,83 +261,97 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, frame, map_, fluid, jitter, budget_s=12.0):
-    """The oracle port on all host threads: rows of the same frame, as many as fit the budget."""
+def cpu_baseline(frame, map_, fluid, jitter, seed):
+    """The oracle port (the reference's lensTrace in scalar C, bit for bit) on all host threads over the
+    whole frame: one untimed frame, then the better of two."""
     from oracle import binding
     threads = binding.oracle().oracleThreads()
-    rows = 8
-    t0 = time.perf_counter()
-    binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads, rows=(536, 544))
-    dt = time.perf_counter() - t0
-    rays_per_s = rows * scene.width * jitter / dt
-    total = int(min(scene.height, max(8, budget_s * rays_per_s / (scene.width * jitter))))
-    y0 = max(0, scene.height // 2 - total // 2)
-    t0 = time.perf_counter()
-    hdr = binding.render32(frame, map_, fluid, jitter=jitter, seed=scene.jitter_seed, threads=threads,
-                           rows=(y0, y0 + total))
-    dt = time.perf_counter() - t0
-    return {"value": total * scene.width * jitter / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"rows {y0}..{y0 + total} of the 1920x1080 frame, {jitter} jittered rays a pixel "
-                      f"({total * scene.width * jitter} geodesics, {dt:.1f} s); the oracle port, scalar C, "
-                      f"{threads} threads"}, hdr[y0:y0 + total], (y0, y0 + total)
+    geodesics = int(frame.size[0]) * int(frame.size[1]) * jitter
+    binding.render32(frame, map_, fluid, jitter=jitter, seed=seed, threads=threads)
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        binding.render32(frame, map_, fluid, jitter=jitter, seed=seed, threads=threads)
+        times.append(time.perf_counter() - t0)
+    dt = min(times)
+    return {"value": geodesics / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the whole 1920x1080 frame, {jitter} jittered rays a pixel ({geodesics} geodesics, "
+                      f"{dt:.2f} s); the oracle port, scalar C, {threads} threads (the reference's AVX2 build "
+                      f"ran {REFERENCE_SIMD_X86['avx2_over_port']}x the port on an x86 host)"}
 
 
-def vs_reference_cpu(gpu, cpu, rows):
+def vs_reference_cpu(frame, map_, fluid, image, jitter, seed):
     """The GPU frame against the reference's CPU trace of the same rays (the oracle port, the reference's
-    bits): pixel classes (disc / sky / horizon) outside one pixel of the photon ring, and the radiance's
-    relative error (of the RGB sum, floor 1e-3)."""
-    bits_gpu = gpu[rows[0]:rows[1], :, 3].astype(np.uint32)
-    bits_cpu = cpu[..., 3].astype(np.uint32)
-    dark = (bits_cpu & 3) == 0
-    near = np.zeros_like(dark)
-    padded = np.pad(dark, 1, mode="edge")
-    h, w = dark.shape
-    for dy in (-1, 0, 1):
-        for dx in (-1, 0, 1):
-            near |= padded[1 + dy:1 + dy + h, 1 + dx:1 + dx + w] != dark
-    keep = ~near
+    bits) and against the same algorithm in FP64 (oracle/parity.py): classes outside the photon ring,
+    radiance within 1e-3 outside the ring and on the pixels resolved at FP32's precision, and the
+    reference's own FP32 against its FP64 beside it."""
+    from oracle import parity
+    out = parity.Reference(frame, map_, fluid, jitter, seed).report(image)
+    out["reference"] = "the oracle port, the reference's lensTrace bit for bit, whole frame"
+    return out
 
-    def classes(b):
-        return np.where(b & 1, 1, np.where(b & 2, 2, 0))
 
-    agree = float(np.mean(classes(bits_gpu)[keep] == classes(bits_cpu)[keep]))
-    a = gpu[rows[0]:rows[1], :, :3].astype(np.float64).sum(-1)
-    b = cpu[..., :3].astype(np.float64).sum(-1)
-    rel = (np.abs(a - b) / np.maximum(np.abs(b), 1e-3))[keep]
-    return {"rows": list(rows), "class_agreement_outside_ring": agree, "ring_share": float(near.mean()),
-            "radiance_within_1e-3": float(np.mean(rel <= 1e-3)), "radiance_rel_p99": float(np.quantile(rel, 0.99)),
-            "reference": "the oracle port, the reference's lensTrace bit for bit"}
+def reference_inputs():
+    """The headline view's inputs for the CPU arm, without the CUDA library: the frame block the
+    reference's own artfHoleFrame filled (recorded from the reference in the golden fixtures), and the
+    synthetic map from the oracle's library, checked against the recorded hash."""
+    import hashlib
+    from artful_gb300 import capi  # (ctypes layouts only: nothing is loaded)
+    from oracle import binding
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as fh:
+        meta = json.load(fh)
+    frame = capi.HoleFrame.from_buffer_copy(bytes.fromhex(meta["c2_rows"]["frame_hex"]))
+    clamped = capi.BlackHoleDesc.from_buffer_copy(bytes.fromhex(meta["views"]["c2"]["clamped_hex"]))
+    synth = meta["views"]["c2"]["synth"]
+    map_ = binding.synth_map(clamped.discInner, clamped.discOuter, clamped.spin, synth["seed"], synth["emissivity"])
+    if hashlib.sha256(map_.tobytes()).hexdigest() != meta["c2_rows"]["map_sha256"]:
+        raise RuntimeError("the CPU arm's synthetic map differs from the recorded one")
+    return frame, map_, np.ones(binding.FLUID_FLOATS, np.float32)
+
+
+# The reference's own SIMD build against the oracle port, measured on an x86 host where the reference's
+# sources are (the AVX2 kernels: 8 lanes): the headline view with 2 x 2 stratified rays a pixel, best of
+# three, 8 threads each.  The Arm host has the reference's NEON kernels (4 lanes) but not its sources.
+REFERENCE_SIMD_X86 = {"avx2_ms": 160.9, "port_ms": 1643.1, "reference_portable_ms": 1228.7, "threads": 8,
+                      "avx2_over_port": 10.2, "view": "1920x1080, 2x2 stratified rays a pixel, a=0.998, i=85 deg",
+                      "same_bits": True}
 
 
 def run_reference(args, rank, world):
-    from artful_gb300 import capi, scenes
+    """The reference's CPU path of the headline workload on this host's cores: every step one whole frame
+    (1920 x 1080, 4 jittered rays a pixel) through the oracle port, the reference's lensTrace restated in
+    scalar C and equal to it bit for bit, on all host threads.  Rank 0 alone; no CUDA library is loaded."""
     if rank != 0:
         return
-    scene = scenes.config2(4)
-    frame, frame64, clamped = scenes.frame(scene)
-    map_ = scenes.synth_map(capi.load(), clamped, scene.seed, scene.emissivity)
-    fluid = scenes.unit_fluid()
     from oracle import binding
+    frame, map_, fluid = reference_inputs()
     threads = binding.oracle().oracleThreads()
-    rows = 16
-    values = []
-    for k in range(args.warmup + args.steps):
-        y0 = (k * rows * 7) % (scene.height - rows)
-        t0 = time.perf_counter()
-        binding.render32(frame, map_, fluid, jitter=4, seed=scene.jitter_seed, threads=threads, rows=(y0, y0 + rows))
-        dt = time.perf_counter() - t0
-        if k >= args.warmup:
-            values.append(rows * scene.width * 4 / dt)
-    value = statistics.median(values)
+    geodesics = 1920 * 1080 * 4
+    for _ in range(args.warmup):
+        binding.render32(frame, map_, fluid, jitter=4, seed=1, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        binding.render32(frame, map_, fluid, jitter=4, seed=1, threads=threads)
+    step_s = (time.perf_counter() - t0) / args.steps
+    value = geodesics / step_s
+    sample = (f"the whole 1920x1080 frame, 4 jittered rays a pixel ({geodesics} geodesics) a step; the oracle "
+              f"port (the reference's lensTrace in scalar C, bit for bit) on {threads} threads.  It stands in for "
+              f"the reference's NEON build, whose sources are not on this host; on an x86 host the reference's "
+              f"AVX2 build ran this view {REFERENCE_SIMD_X86['avx2_over_port']}x the port "
+              f"({REFERENCE_SIMD_X86['avx2_ms']} against {REFERENCE_SIMD_X86['port_ms']} ms, 8 threads)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows * scene.width * 4 / value * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_per_step": f"{rows} rows x 1920 x 4 rays"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{rows} rows of the frame a step; the reference's sources are not on "
-                                       "this host, so its algorithm runs as the oracle port (scalar C)"},
+            "config": bench_config(world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "reference_simd_x86": REFERENCE_SIMD_X86,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def bench_config(world):
+    """The workload both arms name."""
+    return {"workload": WORKLOAD, "parallelism": f"replicas{world}"}
 
 
 def main():
@@ -359,7 +375,9 @@ def main():
     stream = torch.cuda.ExternalStream(lib.artfCudaStream(ctx), device=f"cuda:{local}")
 
     scene = scenes.config2(4)
-    frame, frame64, clamped = scenes.frame(scene)
+    # the reference's own frame block: the traces that work in double widen it (a NULL FP64 frame), so
+    # every trace here and the reference's CPU trace follow the same rays
+    frame, _, clamped = scenes.frame(scene)
     map_ = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
     fluid = scenes.unit_fluid()
     capi.check(lib.artfCudaSetMap(ctx, map_.ctypes.data, 1))
@@ -376,7 +394,7 @@ def main():
         o = opts(precision)
         with torch.cuda.stream(stream):
             for _ in range(warmup):
-                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(o),
                                                  hdr.data_ptr(), None, None))
             stream.synchronize()
             barrier(world)
@@ -385,7 +403,7 @@ def main():
                 flush.fill_(1)
                 start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 start.record(stream)
-                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(o),
                                                  hdr.data_ptr(), None, None))
                 stop.record(stream)
                 stop.synchronize()
@@ -396,7 +414,7 @@ def main():
 
     def stats_of(precision):
         s = capi.TraceStats()
-        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(opts(precision)),
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(opts(precision)),
                                          hdr.data_ptr(), None, C.byref(s)))
         return s
 
@@ -420,10 +438,9 @@ def main():
     def ends_of(precision, step_scale=1.0):
         e = torch.empty((geodesics * 32,), dtype=torch.uint8, device="cuda")
         o = opts(precision, step_scale)
-        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), C.byref(frame64), None, None, C.byref(o),
+        capi.check(lib.artfCudaHoleTrace(ctx, C.byref(frame), None, None, None, C.byref(o),
                                          hdr.data_ptr(), e.data_ptr(), None))
         torch.cuda.synchronize()
-        from oracle.binding import END_DTYPE
         return np.frombuffer(e.cpu().numpy().tobytes(), END_DTYPE), hdr.cpu().numpy().copy()
 
     endpoint = {}
@@ -461,12 +478,12 @@ def main():
     pin_hdr = torch.empty((h, w, 4), dtype=torch.float32).pin_memory()
     o = opts(capi.MIXED)
     for _ in range(args.warmup):
-        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), C.byref(frame64), pin_map.data_ptr(), 0,
+        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), None, pin_map.data_ptr(), 0,
                                           pin_fluid.data_ptr(), 0, C.byref(o), pin_hdr.data_ptr(), None))
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), C.byref(frame64), pin_map.data_ptr(), 0,
+        capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), None, pin_map.data_ptr(), 0,
                                           pin_fluid.data_ptr(), 0, C.byref(o), pin_hdr.data_ptr(), None))
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
 
@@ -474,8 +491,8 @@ def main():
     batch = None
     adjoint = fitting = next_rows = None
     if rank == 0 and not args.quick:
-        cpu, cpu_rows, rows = cpu_baseline(scene, frame, map_, fluid, rays)
-        versus_cpu = vs_reference_cpu(img_mixed, cpu_rows, rows)
+        cpu = cpu_baseline(frame, map_, fluid, rays, scene.jitter_seed)
+        versus_cpu = vs_reference_cpu(frame, map_, fluid, img_mixed, rays, scene.jitter_seed)
         batch = batch_measurement(lib, ctx, args.steps, flush)
         adjoint = adjoint_measurement(lib, ctx, args.steps, flush)
         fitting = fit_measurement(lib, ctx, args.fd_fits)
@@ -488,9 +505,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "mixed",
-                   "parallelism": f"replicas{world}", "l2": "flushed (256 MB write) before every timed step"},
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "precision": "mixed",
+        "config": bench_config(world), "l2": "flushed (256 MB write) before every timed step",
         "mixed_over_fp64": side["fp64"]["ms_per_frame"] / ms_mixed,
         "steps_per_s": s_mixed.steps / (ms_mixed * 1e-3) * world,
         "fp64_step_share": s_mixed.fp64Steps / max(1, s_mixed.steps),
@@ -737,35 +753,6 @@ def batch_measurement(lib, ctx, steps, flush):
             "autotune": {"blockSize": tuning.blockSize, "compactEvery": tuning.compactEvery,
                          "fp64Batch": tuning.fp64Batch, "refillBatch": tuning.refillBatch,
                          "tuned_ms": tuning.ms, "default_ms": tuning.defaultMs, "trials": tuning.trials}}
-
-
-def endpoint_error(e, r, img, img_ref):
-    """Relative endpoint error of each ray against a reference trace: disc-hit radius and azimuth, escape
-    direction, and the pixel's radiance."""
-    both_hit = np.isfinite(e["hitR"]) & np.isfinite(r["hitR"])
-    dr = np.abs(e["hitR"][both_hit] - r["hitR"][both_hit]) / r["hitR"][both_hit]
-    dphi = np.abs(e["hitPhi"][both_hit] - r["hitPhi"][both_hit])
-    dphi = np.minimum(dphi, 1 - dphi)  # turns, on the circle
-    both_sky = ((e["kind"] & 15) == 1) & ((r["kind"] & 15) == 1)
-    ddir = np.linalg.norm(e["dir"][both_sky] - r["dir"][both_sky], axis=1)
-    same_kind = np.mean((e["kind"] & 15) == (r["kind"] & 15))
-    lum = img[..., :3].astype(np.float64).sum(-1)
-    lum_ref = img_ref[..., :3].astype(np.float64).sum(-1)
-    drad = np.abs(lum - lum_ref) / np.maximum(lum_ref, 1e-3)
-    per_ray = np.zeros(len(e))
-    per_ray[both_hit] = np.maximum(dr, dphi)
-    per_ray[both_sky] = np.maximum(per_ray[both_sky], ddir)
-    comparable = both_hit | both_sky
-    q = lambda a, p: float(np.quantile(a, p)) if len(a) else None  # noqa: E731
-    return {
-        "rays_within_1e-4": float(np.mean(per_ray[comparable] <= 1e-4)),
-        "same_end_kind": float(same_kind),
-        "hit_r_rel": {"median": q(dr, .5), "p99": q(dr, .99)},
-        "hit_phi_turns": {"median": q(dphi, .5), "p99": q(dphi, .99)},
-        "escape_dir": {"median": q(ddir, .5), "p99": q(ddir, .99)},
-        "radiance_rel": {"median": q(drad.ravel(), .5), "p99": q(drad.ravel(), .99),
-                         "pixels_within_1e-3": float(np.mean(drad <= 1e-3))},
-    }
 
 
 if __name__ == "__main__":

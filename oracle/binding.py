@@ -94,6 +94,7 @@ def oracle() -> C.CDLL:
         lib.oracleFluidFree.argtypes = [vp]
         lib.oraclePaintDisc.argtypes = [vp]
         lib.oracleSetRings.argtypes = [vp, C.c_float, C.c_float, C.c_float]
+        lib.oracleGasSums.argtypes = [C.c_int, vp, vp]
         lib.artfCudaSynthMap.argtypes = [C.POINTER(SynthDesc), vp]
         lib.artfCudaSynthMap.restype = C.c_int
         _oracle = lib
