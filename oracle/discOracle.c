@@ -10,6 +10,7 @@
 #include "oracle.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -167,6 +168,41 @@ void oraclePaintDisc(float* map) {
             map[SKY_AT + y * SKY_W + x] = .0006f + band * band * ease(.3f, .75f, dust) * .006f;
         }
     }
+}
+
+/* The inner half's sum of the unscaled gas two ways: in texel order (hole.c:143-144, the reference's)
+ * and in the order the GPU's painter adds it (`blocks` runs of texels, each run summed by 256 strided
+ * threads and a pairwise tree, then the runs in order), with the float scale each gives.  The gas takes
+ * no disc parameter, so these are the same for every disc. */
+void oracleGasSums(int blocks, double* sums, float* scales) {
+    const size_t texels = (size_t)MAP_W * (MAP_H / 2);
+    float* gas = (float*)malloc(sizeof(float) * texels);
+    for (int y = 0; y < MAP_H / 2; ++y) {
+        const float rho = (float)y / (float)(MAP_H - 1), thin = 1.f - .887f * rho;
+        for (int x = 0; x < MAP_W; ++x) {
+            float turn = (float)x / (float)MAP_W + rho * .09f;
+            turn -= floorf(turn);
+            gas[(size_t)y * MAP_W + x] = gasAt(turn, rho) * thin * thin;
+        }
+    }
+    double ordered = 0;
+    for (size_t i = 0; i < texels; ++i) ordered += gas[i];
+    const size_t per = texels / (size_t)blocks;
+    double tree = 0, part[256];
+    for (int b = 0; b < blocks; ++b) {
+        const float* run = gas + (size_t)b * per;
+        for (int t = 0; t < 256; ++t) {
+            double s = 0;
+            for (size_t i = (size_t)t; i < per; i += 256) s += run[i];
+            part[t] = s;
+        }
+        for (int width = 128; width > 0; width >>= 1)
+            for (int t = 0; t < width; ++t) part[t] += part[t + width];
+        tree += part[0];
+    }
+    free(gas);
+    sums[0] = ordered, sums[1] = tree;
+    scales[0] = (float)((double)texels / ordered), scales[1] = (float)((double)texels / tree);
 }
 
 /* hole.c:186-197: each ring's orbit speed (turns a unit time), heat, and glow */

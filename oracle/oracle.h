@@ -91,6 +91,9 @@ void oracleFluidFree(OracleFluid* f);
 /* The reference's painted disc (discOracle.c, after hole.c:136-178 buildDisc): gas, dust, colours and
  * sky into a whole map (ring tables left as they are); and the ring tables for a disc (hole.c:186). */
 void oraclePaintDisc(float* map);
+/* The unscaled gas's inner-half sum in texel order and in the GPU painter's order (`blocks` runs), and
+ * the float scale each gives (sums[2], scales[2]). */
+void oracleGasSums(int blocks, double* sums, float* scales);
 void oracleSetRings(float* map, float inner, float outer, float spin);
 
 #endif

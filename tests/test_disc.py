@@ -62,3 +62,22 @@ def test_oracle_painted_map_equals_the_reference_live(oracle_lib, painted):
     m = painted.copy()
     oracle_lib.oracleSetRings(m.ctypes.data, clamped.discInner, clamped.discOuter, clamped.spin)
     np.testing.assert_array_equal(m.view(np.uint32), want.view(np.uint32))
+
+
+def test_gas_scale_is_the_same_float_in_the_gpus_order(oracle_lib):
+    """The painted gas takes no disc parameter, so its inner-half scale is one number for every disc.
+    Its 2^20 float texels add up exactly in double in any order (each has a 24-bit significand, and the
+    partial sums never need more than double's 53 bits at these magnitudes): the GPU painter's order
+    (1024 runs, strided threads and a tree) and the reference's texel order give the same double, hence
+    the same float scale, which lies well away from float's rounding boundary."""
+    import ctypes as C
+    sums = (C.c_double * 2)()
+    scales = (C.c_float * 2)()
+    oracle_lib.oracleGasSums(1024, sums, scales)
+    assert sums[0] == sums[1] and scales[0] == scales[1]
+    texels = 2048 * 512
+    q = [texels / sums[0], texels / sums[1]]
+    f = np.float32(q[0])
+    ulp = float(np.spacing(f))
+    margin = min(abs(q[0] - (float(f) - ulp / 2)), abs(q[0] - (float(f) + ulp / 2)))
+    assert abs(q[0] - q[1]) * 1e6 < margin, (q, margin)
