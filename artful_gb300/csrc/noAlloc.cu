@@ -9,10 +9,15 @@
  *
  * The array lives on every GPU that loads the library until the process exits (74 KB).  Host code
  * cannot use the array's name as a device address, so the first call on each device looks the address
- * up there (cudaGetSymbolAddress, with that device current) and keeps it: make that first call before
- * any stream capture.  All calls share the array and it keeps the last call's contents; each call
- * writes the table and clears the counters before its launch.  Calls whose work overlaps on the GPU
- * (on different streams, or from different threads) race on the array: order them on one stream. */
+ * up there (cudaGetSymbolAddress, with that device current) and keeps it; after a device reset
+ * (cudaDeviceReset, or a reset of the primary context) the kept address is stale, and the process must
+ * restart before it calls this entry point again.  All calls share the array and it keeps the last
+ * call's contents; each call writes the table and clears the counters before its launch.  Calls whose
+ * work overlaps on the GPU (on different streams, or from different threads) race on the array: order
+ * them on one stream.  The table is built in a file-scope host buffer, not on the caller's stack (a
+ * render thread may have a small one), under a lock held until its copy has been staged.  A call made
+ * while its stream is being captured is refused: the graph would record a copy from that host buffer,
+ * which later calls overwrite, and the stats read would end the capture. */
 #include "nvtxRange.h"
 #include "artful_cuda.h"
 #include "lensLaunch.h"
@@ -40,6 +45,10 @@ static __device__ __align__(256) unsigned char noAllocScratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex setupLock;
 void* scratchOn[kMaxDevices]; /* device address of the array, per device; NULL until looked up */
+/* The view table's host side, built and copied under stageLock (a copy from pageable memory is staged
+ * before cudaMemcpyAsync returns, so the buffer is free again once the lock is released). */
+std::mutex stageLock;
+alignas(16) unsigned char stage[ARTF_CUDA_NOALLOC_MAX_VIEWS * artf::kMixedViewBytesMax];
 
 /* The array's device address on the current device, looked up on the first call there. */
 int scratchAddress(int device, unsigned char** out) {
@@ -80,6 +89,11 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
             return artf::failWith(ARTF_CUDA_EINVAL, line);
         }
     }
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &capturing) != cudaSuccess ||
+        capturing != cudaStreamCaptureStatusNone)
+        return artf::failWith(ARTF_CUDA_EINVAL, "the allocation-free batch is not made for a stream being captured "
+                                                "(use the graph API: artfCudaBatchGraphCreate)");
     int device = 0, sms = 0;
     if (cudaGetDevice(&device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
@@ -102,9 +116,8 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     l.smCount = sms;
     l.stream = (cudaStream_t)stream;
 
-    /* the table, built on this thread's stack and copied in (a copy from pageable memory is staged
-     * before the call returns, so the stack buffer may go) */
-    alignas(16) unsigned char stage[ARTF_CUDA_NOALLOC_MAX_VIEWS * artf::kMixedViewBytesMax];
+    /* the table, built in the file's host buffer and copied in */
+    std::unique_lock<std::mutex> staging(stageLock);
     long long units = 0, tiles = 0;
     for (int i = 0; i < count; ++i) {
         /* (no ray planes nor heavy-first order: the fixed scratch cannot hold them, so a work unit is a
@@ -119,6 +132,7 @@ extern "C" int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, co
     unsigned char* table = scratch + kCounterBytes;
     cudaError_t e = cudaMemcpyAsync(table, stage, artf::mixedViewBytes() * (size_t)count, cudaMemcpyHostToDevice,
                                     l.stream);
+    staging.unlock();
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kCounterBytes, l.stream);
     if (e == cudaSuccess) e = artf::launchMixedTable(l, table, count, (int)units, 0, (int)tiles, nullptr, nullptr);
     if (e != cudaSuccess) {

@@ -99,7 +99,9 @@ typedef enum ArtfCudaStatus {
     ARTF_CUDA_ENOMEM = -3,     /* a device allocation failed */
     ARTF_CUDA_ELAUNCH = -4,    /* a launch or copy failed; the context should be destroyed */
     ARTF_CUDA_ETIMEOUT = -5,   /* a bounded device wait gave up (the persistent queue) */
-    ARTF_CUDA_ELOST = -6       /* the context was marked lost (a fault injected on the host) */
+    ARTF_CUDA_ELOST = -6,      /* the context was marked lost (a fault injected on the host) */
+    ARTF_CUDA_EBOUNDS = -7     /* (the debug build, ARTF_CUDA_DEBUG_BOUNDS) an index outside its table or
+                                * frame: the read was kept inside the buffer and the write skipped */
 } ArtfCudaStatus;
 
 /* A line about the last error of this thread's calls; borrowed. */
@@ -321,10 +323,14 @@ void artfCudaBatchGraphDestroy(ArtfCudaGraph* graph);
  * fluid and hdr must be device pointers the caller owns.  Its scratch (the view table and the queue
  * counters) is one fixed array on each device that loads the library, held until the process exits
  * (74 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
- * ARTF_CUDA_EINVAL.  The first call on each device looks up the array's device address there; make it
- * before any stream capture.  Calls share the array: calls whose work overlaps on the GPU race, so order
- * them on one stream.  Asynchronous; stats, when given, synchronises the stream and fills the counts
- * (not ms or flops). */
+ * ARTF_CUDA_EINVAL.  No room is left for ray planes or the heavy-first order: each work unit is a pixel,
+ * whose rays one lane traces in turn, in pixel order (options->order is ignored), which can be slower
+ * than the context's batch for views of several rays a pixel.  The first call on each device looks up
+ * the array's device address there and keeps it; after a device reset the process must restart before
+ * calling this again.  A call on a stream that is being captured is refused (ARTF_CUDA_EINVAL): the
+ * graph API is the form to capture.  Calls share the array: calls whose work overlaps on the GPU race,
+ * so order them on one stream.  Asynchronous; stats, when given, synchronises the stream and fills the
+ * counts (not ms or flops). */
 #define ARTF_CUDA_NOALLOC_MAX_VIEWS 64
 int artfCudaHoleBatchNoAlloc(const ArtfCudaView* views, int count, const ArtfCudaTraceOptions* options, void* stream,
                              ArtfCudaTraceStats* stats);

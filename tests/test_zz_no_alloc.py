@@ -68,3 +68,30 @@ def test_no_alloc_batch_refuses_what_it_cannot_hold(lib):
     assert b"64 views" in lib.artfCudaLastError()
     no_map = (capi.View * 1)(capi.View(views[0].frame, views[0].frame64, None, views[0].fluid, views[0].hdr, None))
     assert lib.artfCudaHoleBatchNoAlloc(no_map, 1, C.byref(opts), None, None) == -1
+
+
+def test_no_alloc_batch_on_a_caller_stream_and_refused_in_a_capture(lib, ctx):
+    """On the caller's own stream the batch is the context batch's; on a stream being captured it is
+    refused (its host staging would be replayed stale), and the capture ends cleanly."""
+    import torch
+    views, keep = _views(lib, 3)
+    opts = capi.TraceOptions(capi.MIXED, 0, 0, 1.0, 0.0, 0, 0, 1)
+    capi.check(lib.artfCudaHoleBatch(ctx, views, len(views), C.byref(opts), None))
+    torch.cuda.synchronize()
+    want = [hdr.cpu().numpy().copy() for _, _, hdr in keep]
+    stream = torch.cuda.Stream()
+    for _, _, hdr in keep:
+        hdr.zero_()
+    torch.cuda.synchronize()
+    capi.check(lib.artfCudaHoleBatchNoAlloc(views, len(views), C.byref(opts), C.c_void_p(stream.cuda_stream), None))
+    stream.synchronize()
+    for i, (_, _, hdr) in enumerate(keep):
+        assert _within_tolerance(hdr.cpu().numpy(), want[i]), i
+    graph = torch.cuda.CUDAGraph()
+    status = None
+    with torch.cuda.graph(graph, stream=stream):
+        keep[0][2].add_(0.0)  # (the capture holds one plain op)
+        status = lib.artfCudaHoleBatchNoAlloc(views, len(views), C.byref(opts), C.c_void_p(stream.cuda_stream), None)
+    assert status == -1
+    assert b"captured" in lib.artfCudaLastError()
+    torch.cuda.synchronize()
