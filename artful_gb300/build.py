@@ -1,7 +1,10 @@
 """Builds libartful_cuda.so in-tree: the C11 host set-up with gcc, the CUDA kernels and the C ABI with
 nvcc for sm_103a only.  Each kernel translation unit carries the float flags that define its rounding.
+With debug=True it builds libartful_cuda_debug.so instead: the same sources with ARTF_CUDA_DEBUG_BOUNDS,
+every table read and frame write checked against its region (lensCore.cuh), the first index outside
+reported by the C ABI as ARTF_CUDA_EBOUNDS.
 
-    python -m artful_gb300.build [--verbose]
+    python -m artful_gb300.build [--verbose] [--debug]
 """
 from __future__ import annotations
 
@@ -17,6 +20,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libartful_cuda.so")
+DEBUG_OBJ = os.path.join(HERE, "_build_debug")
+DEBUG_LIB = os.path.join(HERE, "libartful_cuda_debug.so")
+DEBUG = ["-DARTF_CUDA_DEBUG_BOUNDS"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -58,15 +64,16 @@ def _run(cmd, verbose):
     return r.stdout + r.stderr
 
 
-def build(verbose: bool = False, ptxas_info: bool = False) -> str:
-    os.makedirs(OBJ, exist_ok=True)
+def build(verbose: bool = False, ptxas_info: bool = False, debug: bool = False) -> str:
+    obj, lib = (DEBUG_OBJ, DEBUG_LIB) if debug else (OBJ, LIB)
+    os.makedirs(obj, exist_ok=True)
     jobs = []
     for name, flags in UNITS.items():
-        out = os.path.join(OBJ, name + ".o")
-        extra = ["-Xptxas", "-v"] if ptxas_info else []
+        out = os.path.join(obj, name + ".o")
+        extra = (["-Xptxas", "-v"] if ptxas_info else []) + (DEBUG if debug else [])
         jobs.append([nvcc()] + NVCC_COMMON + flags + extra + ["-c", os.path.join(CSRC, name), "-o", out])
     for name in C_UNITS:
-        out = os.path.join(OBJ, name + ".o")
+        out = os.path.join(obj, name + ".o")
         jobs.append([os.environ.get("CC", "gcc")] + CFLAGS + ["-c", os.path.join(CSRC, name), "-o", out])
     with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as pool:
         logs = list(pool.map(lambda c: _run(c, verbose), jobs))
@@ -74,9 +81,9 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         for log in logs:
             print(log)
     objs = [j[-1] for j in jobs]
-    _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"], verbose)
-    return LIB
+    _run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lpthread"], verbose)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="--verbose" in sys.argv, ptxas_info="--ptxas" in sys.argv))
+    print(build(verbose="--verbose" in sys.argv, ptxas_info="--ptxas" in sys.argv, debug="--debug" in sys.argv))

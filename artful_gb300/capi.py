@@ -10,6 +10,8 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libartful_cuda.so")
+DEBUG_LIB_PATH = os.path.join(HERE, "libartful_cuda_debug.so")  # the bounds-checked build (build --debug)
+EBOUNDS = -7
 
 MAP_WIDTH, MAP_HEIGHT = 2048, 1024
 DUST_WIDTH, DUST_HEIGHT = 1024, 256

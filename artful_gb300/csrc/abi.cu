@@ -73,6 +73,8 @@ struct ArtfCuda {
     size_t adjResultViews;
     void* adjOrder;               /* the adjoint's heavy-first tile order (artf::adjointOrderBytes) */
     size_t adjOrderBytes;
+    void* adjTrail;               /* the rays' kept states between the adjoint's kernels (artf::adjointTrailBytes) */
+    size_t adjTrailBytes;
     uint32_t lastBands; /* launches of the last trace (1 but for a frame in bands) */
     int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
     bool lost;
@@ -158,6 +160,7 @@ extern "C" void artfCudaDestroy(ArtfCuda* ctx) {
     cudaFree(ctx->adjResults);
     cudaFreeHost(ctx->adjResultsHost);
     cudaFree(ctx->adjOrder);
+    cudaFree(ctx->adjTrail);
     if (ctx->start) cudaEventDestroy(ctx->start);
     if (ctx->stop) cudaEventDestroy(ctx->stop);
     if (ctx->staged) cudaEventDestroy(ctx->staged);
@@ -399,6 +402,24 @@ static int readStats(ArtfCuda* ctx, const ArtfCudaHoleFrame& frame, int precisio
     return ARTF_CUDA_OK;
 }
 
+/* The debug build's fault word, read after a trace (ARTF_CUDA_DEBUG_BOUNDS: lensCore.cuh). */
+static int checkBounds(ArtfCuda* ctx) {
+#if defined(ARTF_CUDA_DEBUG_BOUNDS)
+    static const char* const kinds[] = {"", "gas row", "fluid row", "dust row", "sky row", "ring row",
+                                        "colour", "pixel", "ray plane", "ray end"};
+    unsigned long long w[2];
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(w, ctx->counters + artf::CBoundsKind, sizeof w, cudaMemcpyDeviceToHost,
+                                               ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    if (w[0])
+        return fail(ARTF_CUDA_EBOUNDS, "%s index %lld outside its table or frame",
+                    w[0] < sizeof kinds / sizeof kinds[0] ? kinds[w[0]] : "unknown", (long long)w[1]);
+#else
+    (void)ctx;
+#endif
+    return ARTF_CUDA_OK;
+}
+
 /* Frames that go out in bands (vulkan.c:1733-1734): above this many rays, bands of that many. */
 static const int64_t kRaysApart = 64000000, kRaysABand = 8000000;
 
@@ -470,6 +491,7 @@ static int runTrace(ArtfCuda* ctx, artf::TraceLaunch& l, int precision, int64_t 
     if (status) return status;
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = (uint32_t)bands;
+    if ((status = checkBounds(ctx))) return status;
     return stats ? readStats(ctx, l.frame, precision, l.guards, stats) : ARTF_CUDA_OK;
 }
 
@@ -630,7 +652,7 @@ extern "C" int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* par
 }
 
 /* Grows the adjoint's table, staging, block sums and results to `count` views of `blocks` blocks. */
-static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int height) {
+static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int height, int K) {
     if ((size_t)count > ctx->adjViews) {
         cudaFree(ctx->adjTable);
         cudaFreeHost(ctx->adjStage);
@@ -651,7 +673,9 @@ static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int h
     }
     if (int s = reserve((void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float)))
         return s;
-    return reserve(&ctx->adjOrder, &ctx->adjOrderBytes, artf::adjointOrderBytes(count, width, height), 1);
+    if (int s = reserve(&ctx->adjOrder, &ctx->adjOrderBytes, artf::adjointOrderBytes(count, width, height), 1))
+        return s;
+    return reserve(&ctx->adjTrail, &ctx->adjTrailBytes, artf::adjointTrailBytes(count, width, height, K), 1);
 }
 
 extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
@@ -671,7 +695,7 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
                     ARTF_CUDA_ADJOINT_MIN_CHECKPOINT, ARTF_CUDA_ADJOINT_MAX_CHECKPOINT);
     if ((!map && !ctx->mapHeld) || (!fluid && !ctx->fluidHeld)) return fail(ARTF_CUDA_EINVAL, "no map or fluid");
     const int pixels = width * height, blocks = artf::adjointTiles(width, height);
-    if ((status = reserveAdjoint(ctx, count, blocks, width, height))) return status;
+    if ((status = reserveAdjoint(ctx, count, blocks, width, height, checkpointEvery))) return status;
     /* (the staging is free: every call ends synchronised) */
     const size_t slot = artf::adjointViewBytes();
     for (int v = 0; v < count; ++v) {
@@ -691,7 +715,8 @@ extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* para
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * artf::CCount, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->start, ctx->stream));
     const cudaError_t e = artf::launchAdjoint(ctx->adjTable, count, width, height, checkpointEvery, ctx->counters,
-                                              ctx->adjPartials, ctx->adjResults, ctx->stream, ctx->adjOrder);
+                                              ctx->adjPartials, ctx->adjResults, ctx->stream, ctx->adjOrder,
+                                              ctx->adjTrail);
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "adjoint launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(ctx->adjResultsHost, ctx->adjResults, sizeof(double) * 8 * count,
@@ -783,6 +808,7 @@ extern "C" int artfCudaHoleBatch(ArtfCuda* ctx, const ArtfCudaView* views, int c
     if (e != cudaSuccess) return fail(ARTF_CUDA_ELAUNCH, "batch launch: %s", cudaGetErrorString(e));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
+    if ((status = checkBounds(ctx))) return status;
     return stats ? readStats(ctx, views[0].frame, ARTF_CUDA_MIXED, l.guards, stats) : ARTF_CUDA_OK;
 }
 
@@ -900,6 +926,7 @@ extern "C" int artfCudaBatchGraphLaunch(ArtfCudaGraph* g, ArtfCudaTraceStats* st
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaGraphLaunch(g->exec, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaEventRecord(ctx->stop, ctx->stream));
     ctx->lastBands = 1;
+    if ((status = checkBounds(ctx))) return status;
     return stats ? readStats(ctx, g->first, ARTF_CUDA_MIXED, g->options.guards, stats) : ARTF_CUDA_OK;
 }
 

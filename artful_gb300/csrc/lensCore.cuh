@@ -63,27 +63,38 @@ ARTF_HD int32_t clampI(int32_t i, int32_t lo, int32_t hi) { return i < lo ? lo :
 
 /* Division, reciprocal and square roots.  In float these are the plain operations: the unit's flags
  * decide their rounding (IEEE in the exact trace).  In double, units that define ARTF_FAST_FP64 take the
- * hardware's 20-bit estimates (PTX rcp.approx.ftz.f64, rsqrt.approx.f64) and refine them by two
+ * hardware's 20-bit estimates (PTX rcp.approx.ftz.f64, rsqrt.approx.f64) and refine them by
  * Newton-Raphson iterations, each doubling the correct bits (e = 1 - x y, y += y e for the reciprocal;
- * e = 1 - x y^2, y += y e / 2 for the inverse square root): within an ulp or two of the IEEE result,
- * for a fraction of the FP64 instructions of the correctly rounded sequences.  Operands here are
- * normal and positive where square roots are taken. */
+ * e = 1 - x y^2, y += y e / 2 for the inverse square root): two of them (the default) land within an ulp
+ * or two of the IEEE result, for a fraction of the FP64 instructions of the correctly rounded sequences;
+ * a unit that defines ARTF_FP64_NEWTON_STEPS 1 takes one, about 40 correct bits, where the result only
+ * has to be far finer than float's 24.  Operands here are normal and positive where square roots are
+ * taken. */
 #if defined(__CUDA_ARCH__) && defined(ARTF_FAST_FP64)
+#ifndef ARTF_FP64_NEWTON_STEPS
+#define ARTF_FP64_NEWTON_STEPS 2
+#endif
 __device__ __forceinline__ double recipR(double x) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
     double e = fma(-x, y, 1.0);
     y = fma(y, e, y);
+#if ARTF_FP64_NEWTON_STEPS > 1
     e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    y = fma(y, e, y);
+#endif
+    return y;
 }
 __device__ __forceinline__ double invSqrtR(double x) {
     double y;
     asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
     double e = fma(-x * y, y, 1.0);
     y = fma(y * .5, e, y);
+#if ARTF_FP64_NEWTON_STEPS > 1
     e = fma(-x * y, y, 1.0);
-    return fma(y * .5, e, y);
+    y = fma(y * .5, e, y);
+#endif
+    return y;
 }
 __device__ __forceinline__ double divR(double a, double b) { return a * recipR(b); }
 #else
@@ -104,6 +115,29 @@ ARTF_HD double divSqrtR(double a, double x) { return a / sqrt(x); }
 ARTF_HD double rootR(double x) { return sqrt(x); }
 #endif
 ARTF_HD float rootR(float x) { return sqrtf(x); }
+
+/* ---- the debug build's bounds checks -------------------------------------------------------------
+ * Built with ARTF_CUDA_DEBUG_BOUNDS, every table row or entry the shading reads is checked against its
+ * own region of the map or fluid (not only the buffer, which the clamps below keep every read inside),
+ * and every write against the frame or buffer it goes to.  The first index found outside is recorded in
+ * the fault word a frame carries (the launch's CBoundsKind, CBoundsIndex counters) and the C ABI
+ * returns ARTF_CUDA_EBOUNDS; the read still goes through the clamp, as in the release build, and the
+ * write is skipped.  In the release build the checks compile to nothing. */
+enum BoundsKind : uint32_t {
+    kBoundsGasRow = 1, kBoundsFluidRow, kBoundsDustRow, kBoundsSkyRow, kBoundsRingRow, kBoundsColour,
+    kBoundsPixel, kBoundsRayPlane, kBoundsRayEnd
+};
+
+ARTF_HD bool inBounds(unsigned long long* fault, uint32_t kind, int64_t i, int64_t count) {
+#if defined(ARTF_CUDA_DEBUG_BOUNDS) && defined(__CUDA_ARCH__)
+    if (i >= 0 && i < count) return true;
+    if (fault && atomicCAS(fault, 0ull, (unsigned long long)kind) == 0ull) atomicExch(fault + 1, (unsigned long long)i);
+    return false;
+#else
+    (void)fault, (void)kind, (void)i, (void)count;
+    return true;
+#endif
+}
 
 /* A read of the read-only map or fluid (through the non-coherent path on the GPU). */
 ARTF_HD float fetch(const float* p, int32_t i) {
@@ -127,6 +161,7 @@ template <typename R> struct Frame {
     R inner, outer, time, thickness, gain, doppler, stars;
     R pixelX, pixelY, share; /* 2/width, 2/height, 1/(rays a pixel) */
     int32_t width, height, side;
+    unsigned long long* fault; /* the debug build's fault word (two counters), or NULL */
     /* The differentiated traces evaluate the two map tables that depend on the scene's parameters (the
      * rings' orbit speed and their glow, (r / inner)^-q) from their formulas, so that the parameters'
      * derivatives flow through them; every other trace reads the tables. */
@@ -145,6 +180,7 @@ template <typename R> struct Frame {
         gain = R(f.look[0]), doppler = R(f.look[1]), stars = R(f.look[2]);
         pixelX = R(f.image[1]), pixelY = R(f.image[2]), share = R(f.image[3]);
         width = (int32_t)sizes.size[0], height = (int32_t)sizes.size[1], side = (int32_t)sizes.size[2];
+        fault = nullptr;
         analyticTables = 0;
         emissivity = R(0);
     }
@@ -514,6 +550,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
         const R rowFloor = minX(floorR(rowPos), R(ARTF_CUDA_MAP_HEIGHT - 2));
         const R rowPart = rowPos - rowFloor;
         const int32_t row0 = truncI(rowFloor), row1 = row0 + 1;
+        inBounds(f.fault, kBoundsGasRow, row0, ARTF_CUDA_MAP_HEIGHT - 1); /* (row0 and row1) */
         const R speed0 = ringSpeedAt(f, map, row0), speed1 = ringSpeedAt(f, map, row1);
         const R turnK = turn + (inside ? rate * ds : R(0));
         const R d0 = rowAt(map, mapCount, 0, ARTF_CUDA_MAP_WIDTH, row0, turnK - speed0 * c.time);
@@ -523,6 +560,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
         const R fluidPos = (inside ? rhoK : R(0)) * R(ARTF_CUDA_FLUID_HEIGHT - 1);
         const R fluidFloor = minX(floorR(fluidPos), R(ARTF_CUDA_FLUID_HEIGHT - 2));
         const int32_t fluidRow = truncI(fluidFloor);
+        inBounds(f.fault, kBoundsFluidRow, fluidRow, ARTF_CUDA_FLUID_HEIGHT - 1); /* (and the row after) */
         const R fluidTurn = turnK - speed0 * fluidTime;
         const R g0 = rowAt(fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow, fluidTurn);
         const R g1 = rowAt(fluid, fluidCount, 0, ARTF_CUDA_FLUID_WIDTH, fluidRow + 1, fluidTurn);
@@ -531,6 +569,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
         /* dust: less light, more opacity */
         const R dustPos = (inside ? rhoK : R(0)) * R(ARTF_CUDA_DUST_HEIGHT - 1);
         const int32_t dustRow = truncI(minX(floorR(dustPos), R(ARTF_CUDA_DUST_HEIGHT - 1)));
+        inBounds(f.fault, kBoundsDustRow, dustRow, ARTF_CUDA_DUST_HEIGHT);
         const R dusty = rowAt(map, mapCount, ARTF_CUDA_DUST_AT, ARTF_CUDA_DUST_WIDTH, dustRow, turnK - speed0 * c.time);
         const R lit = R(1) - KF(.97) * dusty;
         /* how far from the disc's middle plane, and what the slice stops and gives */
@@ -547,6 +586,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
     const R rhoCenter = (R(1) - f.inner * x.uc) * rhoScale;
     const R rhoSafe = minX(maxX(rhoCenter, R(0)), R(1));
     const int32_t rowIndex = truncI(rhoSafe * R(ARTF_CUDA_MAP_HEIGHT - 1));
+    inBounds(f.fault, kBoundsRingRow, rowIndex, ARTF_CUDA_MAP_HEIGHT);
     R heat = R(fetch(map, clampI(ARTF_CUDA_ROWS_AT + rowIndex + rowIndex + 1, 0, mapCount - 1)));
     const R gives = ringGlowAt(f, map, rowIndex);
     R light = f.gain * glow * gives;
@@ -564,6 +604,7 @@ template <typename R> ARTF_HD R shadeCrossing(const Frame<R>& f, R rhoScale, con
     }
     const R colorPos = minX(heat * R(ARTF_CUDA_COLORS / 2), R(ARTF_CUDA_COLORS - 1));
     const int32_t color = truncI(colorPos);
+    inBounds(f.fault, kBoundsColour, color, ARTF_CUDA_COLORS);
     const int32_t at = ARTF_CUDA_COLORS_AT + color + color + color;
     sum[0] = sum[0] + light * R(fetch(map, clampI(at, 0, mapCount - 1)));
     sum[1] = sum[1] + light * R(fetch(map, clampI(at + 1, 0, mapCount - 1)));
@@ -594,6 +635,7 @@ template <typename R> ARTF_HD void shadeSky(const Frame<R>& f, const float* map,
     const R heightPos = (dir[2] * KF(.5) + KF(.5)) * R(ARTF_CUDA_SKY_HEIGHT - 1);
     const R skyFloor = minX(floorR(heightPos), R(ARTF_CUDA_SKY_HEIGHT - 2));
     const int32_t skyRow = truncI(skyFloor);
+    inBounds(f.fault, kBoundsSkyRow, skyRow, ARTF_CUDA_SKY_HEIGHT - 1); /* (and the row after) */
     const R s0 = rowAt(map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH, skyRow, skyTurn);
     const R s1 = rowAt(map, ARTF_CUDA_MAP_FLOATS, ARTF_CUDA_SKY_AT, ARTF_CUDA_SKY_WIDTH, skyRow + 1, skyTurn);
     const R dust = s0 + (s1 - s0) * (heightPos - skyFloor);

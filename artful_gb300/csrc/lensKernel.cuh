@@ -136,11 +136,16 @@ template <typename R> __device__ __forceinline__ void tracePixel(const KernelPar
         float nx, ny, moment;
         samplePosition(p.h, p.jitter, p.seed, x, y, k, &nx, &ny, &moment);
         const float time = p.h.disc[2] + p.h.spin[3] * moment;
-        ArtfCudaRayEnd* end = p.ends ? p.ends + pixel * (size_t)p.rays + (size_t)k : nullptr;
+        const int64_t endAt = (int64_t)pixel * p.rays + k;
+        ArtfCudaRayEnd* end = p.ends && inBounds(p.f.fault, kBoundsRayEnd, endAt,
+                                                 (int64_t)p.f.width * p.f.height * p.rays)
+                                  ? p.ends + endAt
+                                  : nullptr;
         bits |= classBits(traceRay(p, R(nx), R(ny), R(time), sum, end, t));
     }
     const R share = R(p.share);
-    p.hdr[pixel] = make_float4((float)(sum[0] * share), (float)(sum[1] * share), (float)(sum[2] * share), (float)bits);
+    if (inBounds(p.f.fault, kBoundsPixel, (int64_t)pixel, (int64_t)p.f.width * p.f.height))
+        p.hdr[pixel] = make_float4((float)(sum[0] * share), (float)(sum[1] * share), (float)(sum[2] * share), (float)bits);
 }
 
 /* One warp per 8 x 4 tile, one thread per pixel. */
@@ -196,6 +201,7 @@ template <typename R> cudaError_t launchUniform(const TraceLaunch& l, const void
     KernelParams<R> p;
     if (sizeof(R) == 8) p.f.load(*(const ArtfCudaHoleFrame64*)frameSource, l.frame);
     else p.f.load(*(const ArtfCudaHoleFrame*)frameSource, l.frame);
+    p.f.fault = l.counters + CBoundsKind;
     p.h = l.frame;
     p.map = l.map;
     p.fluid = l.fluid;

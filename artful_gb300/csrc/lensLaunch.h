@@ -9,10 +9,11 @@
 
 namespace artf {
 
-/* Device counters a trace adds to (unsigned 64-bit each). */
+/* Device counters a trace adds to (unsigned 64-bit each).  CBoundsKind and CBoundsIndex: in the
+ * debug build (ARTF_CUDA_DEBUG_BOUNDS), the first index found outside its table or frame (kind, index). */
 enum Counter {
     CRays, CSteps, CCrossings, CEscapes, CFp64Steps, CQueue, CStatus,
-    CFp64Horizon, CFp64Radial, CFp64Polar, CFp64Rounds, CCount
+    CFp64Horizon, CFp64Radial, CFp64Polar, CFp64Rounds, CBoundsKind, CBoundsIndex, CCount
 };
 
 struct TraceLaunch {

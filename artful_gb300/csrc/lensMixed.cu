@@ -562,20 +562,27 @@ __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView
                 const unsigned ended = mixedAdvance(p, guards, *v, r, o);
                 if (ended) {
                     const size_t index = (size_t)y * (size_t)v->f.width + (size_t)x;
-                    ArtfCudaRayEnd* end = v->ends ? v->ends + index * (size_t)v->rays + (size_t)k : nullptr;
+                    const int64_t pixels = (int64_t)v->f.width * v->f.height;
+                    ArtfCudaRayEnd* end = v->ends && inBounds(v->f.fault, kBoundsRayEnd,
+                                                              (int64_t)(index * (size_t)v->rays + (size_t)k),
+                                                              pixels * v->rays)
+                                              ? v->ends + index * (size_t)v->rays + (size_t)k
+                                              : nullptr;
                     const unsigned rayBits = classBits(mixedFinish(r, ended, end, t));
                     live = false;
                     if (v->rayOut) {
                         /* (a plane holds the band's pixels) */
                         const size_t plane = (size_t)v->f.width * (size_t)v->rows;
                         const size_t inBand = (size_t)(y - v->rowBegin) * (size_t)v->f.width + (size_t)x;
-                        v->rayOut[(size_t)k * plane + inBand] =
-                            make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
+                        if (inBounds(v->f.fault, kBoundsRayPlane, (int64_t)((size_t)k * plane + inBand),
+                                     (int64_t)plane * v->rays))
+                            v->rayOut[(size_t)k * plane + inBand] =
+                                make_float4(r.sum[0], r.sum[1], r.sum[2], (float)rayBits);
                         ++k;
                     } else {
                         bits |= rayBits;
                         for (int c = 0; c < 3; ++c) pixel[c] = pixel[c] + r.sum[c];
-                        if (++k == kEnd)
+                        if (++k == kEnd && inBounds(v->f.fault, kBoundsPixel, (int64_t)index, pixels))
                             v->hdr[index] = make_float4(pixel[0] * v->share, pixel[1] * v->share,
                                                         pixel[2] * v->share, (float)bits);
                     }
@@ -627,8 +634,9 @@ __global__ void __launch_bounds__(256) mixedCombine(const MixedView* views) {
         sum[0] = sum[0] + q.x, sum[1] = sum[1] + q.y, sum[2] = sum[2] + q.z;
         bits |= (unsigned)q.w;
     }
-    v.hdr[(size_t)v.rowBegin * (size_t)v.f.width + i] =
-        make_float4(sum[0] * v.share, sum[1] * v.share, sum[2] * v.share, (float)bits);
+    const size_t at = (size_t)v.rowBegin * (size_t)v.f.width + i;
+    if (inBounds(v.f.fault, kBoundsPixel, (int64_t)at, (int64_t)v.f.width * v.f.height))
+        v.hdr[at] = make_float4(sum[0] * v.share, sum[1] * v.share, sum[2] * v.share, (float)bits);
 }
 
 /* The per-ray entry point: rays at given image positions in the table's first view. */
@@ -730,6 +738,7 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     memset(&v, 0, sizeof v);
     v.f.load(frame64, frame);
     v.d.load(frame64, frame);
+    v.f.fault = v.d.fault = l.counters + CBoundsKind;
     v.h = frame;
     v.map = map;
     v.fluid = fluid;
