@@ -47,7 +47,6 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kMaxK = ARTF_CUDA_ADJOINT_MAX_CHECKPOINT;
 constexpr int kMaxSteps = 192;
-constexpr int kMaxSegments = kMaxSteps / ARTF_CUDA_ADJOINT_MIN_CHECKPOINT + 1;
 constexpr float kTurn = .15915494f; /* 1 / 2 pi, the reference's constant */
 
 /* Adjoints of what a ray's constants of motion and the frame's scalars feed. */
@@ -678,11 +677,40 @@ struct alignas(16) Kept {
     float through; /* the disc's transmission before this step's crossing */
 };
 
+/* Each ray's trail from the forward kernel to the reverse one, in device memory, field by field across
+ * rays (a warp's 32 rays are adjacent in every field: its loads and stores coalesce):
+ *   head  (steps, top, escaped, 0) as ints: steps taken, and steps 0 .. top - 1 go back
+ *   bar   (dL/dR, dL/dG, dL/dB, the transmission at the end)
+ *   end   the state after the last step (three float4)
+ *   saved the state at the start of each segment of K steps (three float4 a segment)
+ * A state is (u, w, n0, n1), (n2, v0, v1, v2), (psi, drag, through, 0). */
+struct Trail {
+    int4* head;
+    float4* bar;
+    float4* end;    /* 3 x rays */
+    float4* saved;  /* 3 x segments x rays */
+    size_t rays;
+};
+
+__device__ __forceinline__ void storeState(float4* at, size_t stride, const RayState<float>& s, float through) {
+    at[0] = make_float4(s.u, s.w, s.n[0], s.n[1]);
+    at[stride] = make_float4(s.n[2], s.v[0], s.v[1], s.v[2]);
+    at[2 * stride] = make_float4(s.psi, s.drag, through, 0.f);
+}
+
+__device__ __forceinline__ void loadState(const float4* at, size_t stride, RayState<float>& s, float& through) {
+    const float4 a = at[0], b = at[stride], c = at[2 * stride];
+    s.u = a.x, s.w = a.y, s.n[0] = a.z, s.n[1] = a.w;
+    s.n[2] = b.x, s.v[0] = b.y, s.v[1] = b.z, s.v[2] = b.w;
+    s.psi = c.x, s.drag = c.y, through = c.z;
+}
+
 struct AdjointLaunch {
     const AdjointView* views;
     float* partials; /* 8 floats a tile: the loss, the five gradient components, two unused */
     unsigned long long* counters;
     const int* order; /* each view's tiles, heaviest first (tilesPerView a view), or NULL: in order */
+    Trail trail;
     int tilesX, tilesPerView, totalTiles, K;
 };
 
@@ -699,147 +727,199 @@ __device__ __forceinline__ void stepOnce(const AdjointView& v, float rhoScale, c
     }
 }
 
-/* Pixel i's ray: forward with checkpoints, the loss, back; adds the loss and its gradient to acc. */
-__device__ __forceinline__ void adjointRay(const AdjointView& v, int px, int py, int K, float* acc, Tally& tally) {
-    const Frame<float>& f = v.f;
-    const int i = py * f.width + px;
-    float nx, ny, moment;
+/* The ray of pixel (px, py) at its centre: its image position, constants of motion and first state. */
+__device__ __forceinline__ void adjointStart(const AdjointView& v, int px, int py, float& nx, float& ny,
+                                             RayConst<float>& c, RayState<float>& s) {
+    float moment;
     samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
-    RayConst<float> c;
-    RayState<float> s;
-    rayStart(f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
-    const float a = f.a;
-    if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
-    const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
-    Kept ring[kMaxK + 1];
-    Kept checkpoint[kMaxSegments];
-    /* forward: the segment's states, and each segment's first */
-    float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
-    int steps = 0, lastCrossing = -1;
-    unsigned crossings = 0;
-    bool escaped = false;
-    RayState<float> end = s;
-    for (int step = 0; step < kMaxSteps; ++step) {
-        if (step % K == 0) checkpoint[step / K] = Kept{s, through};
-        ring[step % K] = Kept{s, through};
-        StepOut<float> o;
-        const unsigned crossed = crossings;
-        stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
-        if (crossings != crossed) lastCrossing = step;
-        ++steps;
-        end = o.next;
-        if (0.f > o.next.u) {
-            const float part = s.u / (s.u - o.next.u);
-            float away[3], dir[3];
-            for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
-            skyDirection(away, s.psi + part * (o.next.psi - s.psi), dir);
-            if (f.stars > 0.f) shadeSky(f, v.map, c, dir, through, sum);
-            escaped = true;
-            break;
-        }
-        if (o.next.u > f.uHorizon || !(through > .004f)) break;
-        s = o.next;
-    }
-    const int lastFirst = ((steps - 1) / K) * K;
-    /* the loss, and its adjoint in the radiance */
-    const float4 want = v.target[i];
-    const float diff[3] = {sum[0] - want.x, sum[1] - want.y, sum[2] - want.z};
-    acc[0] += (diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]) * v.lossScale;
-    const float sumBar[3] = {2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale, 2.f * diff[2] * v.lossScale};
-    if (v.hdr) v.hdr[i] = make_float4(sum[0], sum[1], sum[2], 0.f);
-    const float throughEnd = through;
-    /* back, a segment at a time */
-    StepBar next;
-    memset(&next, 0, sizeof next);
-    ConstBar g;
-    memset(&g, 0, sizeof g);
-    float throughBar = 0.f;
-    /* Back from the last step that added to the radiance (the escape, when the sky is shown; else the last
-     * disc crossing): after it every adjoint is zero, and a step taken back with zero adjoints adds exactly
-     * nothing, so those steps, and the recomputation of segments holding only them, are skipped. */
-    const int top = escaped && f.stars > 0.f ? steps : lastCrossing + 1; /* steps 0 .. top - 1 go back */
-    for (int first = top > 0 ? ((top - 1) / K) * K : -K; first >= 0; first -= K) {
-        const int last = min(first + K, top); /* steps first .. last - 1 */
-        /* the state at the segment's end: the ray's, the start of step `last` (in the ring when this is the
-         * ray's last segment), or where the recomputation ends */
-        RayState<float> after = end;
-        if (first == lastFirst && last != steps) after = ring[last - first].s;
-        if (first != lastFirst) {
-            RayState<float> r = checkpoint[first / K].s;
-            float t = checkpoint[first / K].through, junk[3] = {0.f, 0.f, 0.f};
-            unsigned n = 0;
-            for (int step = first; step < last; ++step) {
-                ring[step - first] = Kept{r, t};
-                StepOut<float> o;
-                stepOnce(v, rhoScale, c, r, o, t, junk, n);
-                r = o.next;
-            }
-            after = r;
-        }
-        for (int step = last - 1; step >= first; --step) {
-            const Kept k = ring[step - first];
-            StepOut<float> o;
-            o.next = after;
-            o.k1 = bendAt(c, k.s.u);
-            accelOf(a, c.big, k.s.n, o.a1);
-            StepBar b;
-            memset(&b, 0, sizeof b);
-            b.nextU = next.u;
-            for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
-            b.nextPsi = next.psi;
-            b.nextDrag = next.drag;
-            if (escaped && step == steps - 1 && f.stars > 0.f)
-                skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
-            Crossing<float> x;
-            if (crossingOf(f, rhoScale, c, k.s, o, x))
-                crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
-            radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w, b.psi,
-                       b.drag, g);
-            polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
-            next = b;
-            after = k.s;
-        }
-    }
-    float grad[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    startBack(v, nx, ny, c, next, g, grad);
-    for (int q = 0; q < 5; ++q) acc[1 + q] += grad[q];
-    if (v.pixelGrads)
-        for (int q = 0; q < 5; ++q) v.pixelGrads[(size_t)i * 5 + q] = grad[q];
-    tally.rays += 1;
-    tally.steps += (unsigned)steps;
-    tally.crossings += crossings;
-    tally.escapes += escaped;
+    rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
+    if (v.f.a != 0.f) s.drag = dragAt(v.f.a, v.f.a * v.f.a, c.xiA, s.u);
 }
 
 /* A warp an 8 x 4 tile of pixels (rays of neighbouring pixels take similar numbers of steps, so a warp's
  * lanes stay busy together), a block four tiles of one view (blockIdx.y).  Each warp writes its tile's
  * sums to the tile's own slot and leaves: no warp waits for another once the view is in shared memory.
- * (A persistent grid taking tiles from a device counter measured slower: its warps hold more ray state
- * resident at once.)  kK: the checkpoint interval as a constant (the default, 32: the ring's index and
- * the checkpoint's are then a mask and a shift, not divisions), or 0 to read it from L. */
-template <int kK> __global__ void __launch_bounds__(kThreads) adjointPixels(const AdjointLaunch L) {
-    __shared__ AdjointView v;
-    {
-        const int4* src = reinterpret_cast<const int4*>(L.views + blockIdx.y);
-        int4* dst = reinterpret_cast<int4*>(&v);
-        for (int k = threadIdx.x; k < (int)(sizeof(AdjointView) / 16); k += kThreads) dst[k] = src[k];
-    }
-    __syncthreads();
+ * A tile's rays are trail entries (view * tilesPerView + tile) * 32 + lane. */
+struct TileLane {
+    int local, px, py;
+    size_t tile, ray;
+    bool inside;
+};
+
+__device__ __forceinline__ bool tileLane(const AdjointLaunch& L, const AdjointView& v, TileLane& t) {
     const int lane = (int)(threadIdx.x & 31);
     const int slot = (int)(blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5));
-    if (slot >= L.tilesPerView) return; /* the whole warp: its tile lies past the view */
-    const int local = L.order ? L.order[(size_t)blockIdx.y * L.tilesPerView + slot] : slot;
-    const int px = (local % L.tilesX) * 8 + (lane & 7), py = (local / L.tilesX) * 4 + (lane >> 3);
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (slot >= L.tilesPerView) return false; /* the whole warp: its tile lies past the view */
+    t.local = L.order ? L.order[(size_t)blockIdx.y * L.tilesPerView + slot] : slot;
+    t.px = (t.local % L.tilesX) * 8 + (lane & 7), t.py = (t.local / L.tilesX) * 4 + (lane >> 3);
+    t.tile = (size_t)blockIdx.y * L.tilesPerView + t.local;
+    t.ray = t.tile * 32 + (size_t)lane;
+    t.inside = t.px < v.f.width && t.py < v.f.height;
+    return true;
+}
+
+__device__ __forceinline__ void copyView(const AdjointLaunch& L, AdjointView& v) {
+    const int4* src = reinterpret_cast<const int4*>(L.views + blockIdx.y);
+    int4* dst = reinterpret_cast<int4*>(&v);
+    for (int k = threadIdx.x; k < (int)(sizeof(AdjointView) / 16); k += kThreads) dst[k] = src[k];
+}
+
+/* The forward kernel: each ray traced with its shading, the state kept at the start of every segment of K
+ * steps, the loss and its adjoint in the radiance; the tile's loss to its slot.  kK: the checkpoint
+ * interval as a constant (the default, 32: segment indices are shifts), or 0 to read it from L. */
+template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(const AdjointLaunch L) {
+    __shared__ AdjointView v;
+    copyView(L, v);
+    __syncthreads();
+    TileLane t;
+    if (!tileLane(L, v, t)) return;
+    const int K = kK ? kK : L.K;
+    const Trail& tr = L.trail;
+    float loss = 0.f;
     Tally tally;
-    if (px < v.f.width && py < v.f.height) adjointRay(v, px, py, kK ? kK : L.K, acc, tally);
+    if (t.inside) {
+        const Frame<float>& f = v.f;
+        float nx, ny;
+        RayConst<float> c;
+        RayState<float> s;
+        adjointStart(v, t.px, t.py, nx, ny, c, s);
+        const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
+        float sum[3] = {0.f, 0.f, 0.f}, through = 1.f;
+        int steps = 0, lastCrossing = -1;
+        unsigned crossings = 0;
+        bool escaped = false;
+        RayState<float> end = s;
+        for (int step = 0; step < kMaxSteps; ++step) {
+            if (step % K == 0) storeState(tr.saved + (size_t)(3 * (step / K)) * tr.rays + t.ray, tr.rays, s, through);
+            StepOut<float> o;
+            const unsigned crossed = crossings;
+            stepOnce(v, rhoScale, c, s, o, through, sum, crossings);
+            if (crossings != crossed) lastCrossing = step;
+            ++steps;
+            end = o.next;
+            if (0.f > o.next.u) {
+                const float part = s.u / (s.u - o.next.u);
+                float away[3], dir[3];
+                for (int k = 0; k < 3; ++k) away[k] = s.n[k] + part * (o.next.n[k] - s.n[k]);
+                skyDirection(away, s.psi + part * (o.next.psi - s.psi), dir);
+                if (f.stars > 0.f) shadeSky(f, v.map, c, dir, through, sum);
+                escaped = true;
+                break;
+            }
+            if (o.next.u > f.uHorizon || !(through > .004f)) break;
+            s = o.next;
+        }
+        const float4 want = v.target[t.py * f.width + t.px];
+        const float diff[3] = {sum[0] - want.x, sum[1] - want.y, sum[2] - want.z};
+        loss = (diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]) * v.lossScale;
+        if (v.hdr) v.hdr[t.py * f.width + t.px] = make_float4(sum[0], sum[1], sum[2], 0.f);
+        /* Back from the last step that added to the radiance (the escape, when the sky is shown; else the
+         * last disc crossing): after it every adjoint is zero, and a step taken back with zero adjoints
+         * adds exactly nothing, so those steps, and the recomputation of segments holding only them, are
+         * skipped. */
+        const int top = escaped && f.stars > 0.f ? steps : lastCrossing + 1;
+        tr.head[t.ray] = make_int4(steps, top, escaped ? 1 : 0, 0);
+        tr.bar[t.ray] = make_float4(2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale,
+                                    2.f * diff[2] * v.lossScale, through);
+        storeState(tr.end + t.ray, tr.rays, end, through);
+        tally.rays += 1;
+        tally.steps += (unsigned)steps;
+        tally.crossings += crossings;
+        tally.escapes += escaped;
+    } else {
+        tr.head[t.ray] = make_int4(0, 0, 0, 0);
+    }
     flushTally(tally, L.counters);
-    const size_t tile = (size_t)blockIdx.y * L.tilesPerView + local;
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_down_sync(0xFFFFFFFFu, loss, off);
+    if ((threadIdx.x & 31) == 0) L.partials[t.tile * 8] = loss;
+}
+
+/* The reverse kernel: each ray's steps taken back from its last contributing one, a segment at a time,
+ * each segment recomputed from its kept state into a ring of K states, then the ray's set-up; the tile's
+ * gradient to its slot. */
+template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(const AdjointLaunch L) {
+    __shared__ AdjointView v;
+    copyView(L, v);
+    __syncthreads();
+    TileLane t;
+    if (!tileLane(L, v, t)) return;
+    const int K = kK ? kK : L.K;
+    const Trail& tr = L.trail;
+    float grad[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int4 head = t.inside ? tr.head[t.ray] : make_int4(0, 0, 0, 0);
+    const int steps = head.x, top = head.y;
+    const bool escaped = head.z != 0;
+    if (top > 0) {
+        const Frame<float>& f = v.f;
+        const float a = f.a;
+        float nx, ny;
+        RayConst<float> c;
+        RayState<float> start;
+        adjointStart(v, t.px, t.py, nx, ny, c, start);
+        const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
+        const float4 bar = tr.bar[t.ray];
+        const float sumBar[3] = {bar.x, bar.y, bar.z}, throughEnd = bar.w;
+        Kept ring[kK ? kK : kMaxK];
+        StepBar next;
+        memset(&next, 0, sizeof next);
+        ConstBar g;
+        memset(&g, 0, sizeof g);
+        float throughBar = 0.f;
+        for (int first = ((top - 1) / K) * K; first >= 0; first -= K) {
+            const int last = min(first + K, top); /* steps first .. last - 1 */
+            /* the segment's states from its kept start; the state after its last step is the ray's end
+             * when that step was the ray's last, else one more step on */
+            RayState<float> r;
+            float through;
+            loadState(tr.saved + (size_t)(3 * (first / K)) * tr.rays + t.ray, tr.rays, r, through);
+            float junk[3] = {0.f, 0.f, 0.f};
+            unsigned n = 0;
+            for (int step = first; step < last; ++step) {
+                ring[step - first] = Kept{r, through};
+                if (step == steps - 1) break;
+                StepOut<float> o;
+                stepOnce(v, rhoScale, c, r, o, through, junk, n);
+                r = o.next;
+            }
+            RayState<float> after = r;
+            if (last == steps) {
+                float unused;
+                loadState(tr.end + t.ray, tr.rays, after, unused);
+            }
+            for (int step = last - 1; step >= first; --step) {
+                const Kept k = ring[step - first];
+                StepOut<float> o;
+                o.next = after;
+                o.k1 = bendAt(c, k.s.u);
+                accelOf(a, c.big, k.s.n, o.a1);
+                StepBar b;
+                memset(&b, 0, sizeof b);
+                b.nextU = next.u;
+                for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
+                b.nextPsi = next.psi;
+                b.nextDrag = next.drag;
+                if (escaped && step == steps - 1 && f.stars > 0.f)
+                    skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
+                Crossing<float> x;
+                if (crossingOf(f, rhoScale, c, k.s, o, x))
+                    crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
+                radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w,
+                           b.psi, b.drag, g);
+                polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
+                next = b;
+                after = k.s;
+            }
+        }
+        startBack(v, nx, ny, c, next, g, grad);
+    }
+    if (t.inside && v.pixelGrads)
+        for (int q = 0; q < 5; ++q) v.pixelGrads[(size_t)(t.py * v.f.width + t.px) * 5 + q] = grad[q];
+    const int lane = (int)(threadIdx.x & 31);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        float s = acc[k];
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
-        if (lane == 0) L.partials[tile * 8 + k] = s;
+    for (int q = 0; q < 5; ++q) {
+        float sum = grad[q];
+        for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, off);
+        if (lane == 0) L.partials[t.tile * 8 + 1 + q] = sum;
     }
 }
 
@@ -959,8 +1039,17 @@ size_t adjointOrderBytes(int count, int width, int height) {
     return sizeof(unsigned) * 2 * kClassStride * (size_t)count + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
 }
 
+/* The trail's rays: 32 a tile, padding lanes included. */
+static size_t trailRays(int count, int width, int height) { return (size_t)count * adjointTiles(width, height) * 32; }
+
+static int trailSegments(int K) { return (kMaxSteps + K - 1) / K; }
+
+size_t adjointTrailBytes(int count, int width, int height, int K) {
+    return trailRays(count, width, height) * sizeof(float4) * (2 + 3 + 3 * (size_t)trailSegments(K));
+}
+
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
-                          float* partials, double* results, cudaStream_t stream, void* orderScratch) {
+                          float* partials, double* results, cudaStream_t stream, void* orderScratch, void* trail) {
     AdjointLaunch L;
     L.views = (const AdjointView*)table;
     L.partials = partials;
@@ -970,6 +1059,11 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.tilesPerView = adjointTiles(width, height);
     L.totalTiles = L.tilesPerView * count;
     L.K = K;
+    L.trail.rays = trailRays(count, width, height);
+    L.trail.head = (int4*)trail;
+    L.trail.bar = (float4*)(L.trail.head + L.trail.rays);
+    L.trail.end = L.trail.bar + L.trail.rays;
+    L.trail.saved = L.trail.end + 3 * L.trail.rays;
     if (orderScratch) {
         unsigned* classes = (unsigned*)orderScratch;
         unsigned* cursors = classes + kClassStride * (size_t)count;
@@ -983,8 +1077,14 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
         L.order = order;
     }
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
-    if (K == 32) adjointPixels<32><<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
-    else adjointPixels<0><<<dim3(blocks, (unsigned)count), kThreads, 0, stream>>>(L);
+    const dim3 grid(blocks, (unsigned)count);
+    if (K == 32) {
+        adjointForward<32><<<grid, kThreads, 0, stream>>>(L);
+        adjointReverse<32><<<grid, kThreads, 0, stream>>>(L);
+    } else {
+        adjointForward<0><<<grid, kThreads, 0, stream>>>(L);
+        adjointReverse<0><<<grid, kThreads, 0, stream>>>(L);
+    }
     adjointSums<<<count, 256, 0, stream>>>(partials, L.tilesPerView, results);
     return cudaGetLastError();
 }

@@ -31,9 +31,12 @@ int adjointTiles(int width, int height); /* 8 x 4 tiles of pixels a view */
 void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* jacobian, double emissivity,
                      const float* map, const float* fluid, const float* target, float* hdr, float* pixelGrads);
 /* The adjoint over `count` views of width x height; partials: count * adjointTiles(width, height) * 8
- * floats of scratch; results: count * 8 doubles (the loss, the five gradient components, two unused). */
+ * floats of scratch; results: count * 8 doubles (the loss, the five gradient components, two unused);
+ * trail: adjointTrailBytes of scratch, where the forward kernel leaves each ray's kept states for the
+ * reverse one. */
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
-                          float* partials, double* results, cudaStream_t stream, void* orderScratch);
+                          float* partials, double* results, cudaStream_t stream, void* orderScratch, void* trail);
+size_t adjointTrailBytes(int count, int width, int height, int K);
 /* Device bytes of the adjoint's heavy-first tile order (orderScratch above; NULL: the tiles in order). */
 size_t adjointOrderBytes(int count, int width, int height);
 
