@@ -69,7 +69,92 @@ def parse():
                    help="time the mixed trace's guard, band and batch variants, each with its endpoint error")
     p.add_argument("--fd-fits", type=int, default=4,
                    help="fits of the inverse-fit workload also run with FP64 central-difference gradients")
+    p.add_argument("--gradient-bias", type=int, default=0, metavar="FITS",
+                   help="compare the adjoint's gradient with FP64 central differences of several steps on the "
+                        "first FITS inverse fits, and print the loss along each parameter, then exit")
     return p.parse_args()
+
+
+def gradient_bias(args):
+    """Why the inverse fits do not recover their parameters.  On the first fits of the configuration-5
+    workload (256 x 144, targets from seed 3, starts 15% off): the adjoint's gradient against central
+    differences of the FP64 loss at steps of 1e-2 .. 1e-4 of each parameter, at the start and halfway to
+    the target (cosine per fit, sign agreement and the ratio of the components); and the FP64 loss along
+    the straight line start -> target and along each parameter alone around the target.  One JSON line."""
+    import torch
+    from artful_gb300 import capi, fit, scenes
+    lib = capi.load()
+    ctx = C.c_void_p()
+    capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
+    fits = fit.config5_fits(32, seed=3)[:args.gradient_bias]
+    m = fit.param_map(fits[0][0])
+    capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
+    unit = scenes.unit_fluid()
+    capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 0))
+    w, h = 256, 144
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    targets = adj.render([t for t, _ in fits])
+    fp64 = fit.Fp64Loss(lib, ctx, w, h, m, lib.artfCudaDeviceFluid(ctx), 10 * len(fits))
+
+    def scale_of(p):
+        return np.array([max(abs(x), 1e-1) for x in fit.theta_of(p)])
+
+    def differences(params, step):
+        """Central differences of the FP64 loss, each parameter moved by step times its size."""
+        moved, views = [], []
+        for k, p in enumerate(params):
+            th, sc = fit.theta_of(p), scale_of(p)
+            for q in range(5):
+                for sign in (1.0, -1.0):
+                    t = th.copy()
+                    t[q] += sign * step * sc[q]
+                    moved.append(fit.with_theta(p, fit.project(t)))
+                    views.append(k)
+        out = np.empty(len(moved))
+        for lo in range(0, len(moved), fp64.capacity):
+            idx = torch.tensor(views[lo:lo + fp64.capacity], device="cuda")
+            out[lo:lo + len(moved[lo:lo + fp64.capacity])] = fp64.losses(moved[lo:lo + fp64.capacity],
+                                                                         targets.index_select(0, idx))
+        out = out.reshape(len(params), 5, 2)
+        return (out[..., 0] - out[..., 1]) / (2 * step * np.stack([scale_of(p) for p in params]))
+
+    table = {}
+    for point in ("start", "halfway"):
+        params = [fit.with_theta(s, fit.theta_of(s) if point == "start" else 0.5 * (fit.theta_of(s) + fit.theta_of(t)))
+                  for t, s in fits]
+        _, g_adj, _ = adj(params, targets)
+        sc = np.stack([scale_of(p) for p in params])
+        rows = {}
+        for step in (1e-2, 3e-3, 1e-3, 1e-4):
+            g = differences(params, step)
+            cos = [float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-30)) for a, b in zip(g_adj, g)]
+            with np.errstate(invalid="ignore", divide="ignore"):
+                ratio = np.where(np.abs(g * sc) > 1e-12, (g_adj * sc) / (g * sc), np.nan)
+            rows[f"{step:g}"] = {
+                "median_cosine": float(np.median(cos)),
+                "sign_agreement": dict(zip(fit.PARAM_NAMES, np.mean(np.sign(g_adj) == np.sign(g), 0).tolist())),
+                "median_ratio": dict(zip(fit.PARAM_NAMES, np.nanmedian(ratio, 0).tolist()))}
+        table[point] = rows
+    line = []
+    for frac in np.linspace(0.0, 1.0, 11):
+        params = [fit.with_theta(s, (1 - frac) * fit.theta_of(s) + frac * fit.theta_of(t)) for t, s in fits]
+        line.append(float(np.median(fp64.losses(params, targets))))
+    alone = {}
+    offsets = (-0.15, -0.1, -0.05, -0.02, 0.0, 0.02, 0.05, 0.1, 0.15)
+    for q, name in enumerate(fit.PARAM_NAMES):
+        row = []
+        for frac in offsets:
+            params = []
+            for t, _ in fits:
+                th = fit.theta_of(t).copy()
+                th[q] *= 1 + frac
+                params.append(fit.with_theta(t, fit.project(th)))
+            row.append(float(np.median(fp64.losses(params, targets))))
+        alone[name] = row
+    print(json.dumps({"gradient_bias": table, "fits": len(fits),
+                      "loss_start_to_target_median": line, "loss_alone_offsets": list(offsets),
+                      "loss_alone_median": alone}), flush=True)
+    lib.artfCudaDestroy(ctx)
 
 
 def sweep(args):
@@ -361,6 +446,9 @@ def main():
         return
     if args.sweep:
         sweep(args)
+        return
+    if args.gradient_bias:
+        gradient_bias(args)
         return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
