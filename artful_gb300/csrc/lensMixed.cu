@@ -1,8 +1,11 @@
 /* artful_cuda — the mixed-precision trace: FP32 for the bulk of each geodesic, FP64 only where
  * stability needs it.
  *
- *   MOTION   the constants of motion (E, xi = L_z / E, Carter's eta, K) and the first state come from
- *            the ray at the eye in FP64, from the frame computed in double;
+ *   MOTION   the constants of motion (E, xi = L_z / E, Carter's eta, K and the radial equation's
+ *            coefficients) come from the ray at the eye in FP64, from the frame in double; the first
+ *            state's w and v and the step, the integrator's FP32 quantities, are formed from them in
+ *            FP32 (the step by the reference's rule from the narrowed K, so every sub-step of a ray,
+ *            FP32 or FP64, takes the same one);
  *   HORIZON  within a band of the outer horizon (u > band * 0.995 / r+) the radial sub-step of
  *            (u, du/ds, psi) runs in FP64: Delta / r^2 in the frame-drag rate loses most of its bits to
  *            cancellation there;
@@ -27,6 +30,7 @@
  * lane computes exactly what the per-ray path (traceRayMixed) computes, in the same order: the
  * schedule changes when, never what.  A single frame is a batch of one view. */
 #define ARTF_FAST_FP64 1 /* FP64 division and square roots by refined hardware estimates (lensCore.cuh) */
+#define ARTF_FP64_NEWTON_STEPS 1 /* one refinement: ~40 bits, far below float's rounding (3.4 % faster) */
 #include "lensKernel.cuh"
 #include "lensMixed.h"
 
@@ -50,6 +54,8 @@ struct MixedView {
     double wideA2, wideTwoA2; /* a^2 and 2 a^2 in double, for the FP64 sub-steps */
     StartTerms<double> start64; /* what each ray's FP64 set-up takes from the view alone */
     float startNarrow[4];     /* the eye's e_r and 1/r in float, where every ray's FP64 set-up starts */
+    float wScaleNarrow;       /* -u0^2 sqrt(Delta) sqrt(Sigma), in float: w's factor from the eye */
+    float stepBaseNarrow;     /* the step rule's (pi / 24) x step scale, in float */
     float rhoScale, uGuard, share;
     int tilesX, pixelUnits, units, unitBase, tileBase, rays, jitter;
     int rowBegin, rows; /* the pixel rows this launch traces (a band of the frame, or all of it) */
@@ -137,18 +143,32 @@ __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
 /* A ray's start: its constants of motion and first state, in FP64 under the MOTION guard. */
 __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards, const MixedView& v, float nx,
                                            float ny, float time, MixedRay& r) {
-    if (guards & ARTF_CUDA_GUARD_MOTION) {
+    if ((guards & ARTF_CUDA_GUARD_MOTION) && v.d.boost[3] > 1.0) {
+        /* a moving eye: the whole set-up with its aberration in FP64 */
         RayConst<double> cd;
         RayState<double> sd;
         rayStartWith(v.d, v.start64, widen(nx), widen(ny), widen(time), cd, sd);
-        r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi);
-        r.c.moved = v.d.boost[3] > 1.0 ? narrow(cd.moved) : 1.f; /* (1 for an eye at rest) */
+        r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi), r.c.moved = narrow(cd.moved);
         r.c.big = narrow(cd.big), r.c.step = narrow(cd.step), r.c.uA = narrow(cd.uA), r.c.uB = narrow(cd.uB);
         r.c.uC = narrow(cd.uC), r.c.xiA = narrow(cd.xiA);
         r.big = cd.big, r.step = cd.step, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
-        /* (u and n start at the eye's: the view's, narrowed once) */
         r.s.u = v.startNarrow[3], r.s.w = narrow(sd.w);
         for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = narrow(sd.v[k]);
+    } else if (guards & ARTF_CUDA_GUARD_MOTION) {
+        RayConst<double> cd;
+        MotionFactors<double> m;
+        motionConstants(v.d, v.start64, widen(nx), widen(ny), cd, m);
+        r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi), r.c.moved = 1.f;
+        r.c.big = narrow(cd.big), r.c.uA = narrow(cd.uA), r.c.uB = narrow(cd.uB);
+        r.c.uC = narrow(cd.uC), r.c.xiA = narrow(cd.xiA);
+        r.big = cd.big, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
+        r.c.step = divSqrtR(v.stepBaseNarrow, maxX(r.c.big, 4.f));
+        r.step = widen(r.c.step);
+        /* (u and n start at the eye's: the view's, narrowed once) */
+        const float across = narrow(m.across), xiAxis = narrow(m.xiAxis);
+        r.s.u = v.startNarrow[3];
+        r.s.w = v.wScaleNarrow * narrow(m.dx) * narrow(m.over);
+        for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = across * v.f.etheta[k] + xiAxis * v.f.ephi[k];
     } else {
         rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
         r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
@@ -749,6 +769,8 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.start64 = startTerms(v.d, (double)l.stepScale);
     for (int k = 0; k < 3; ++k) v.startNarrow[k] = (float)v.d.er[k];
     v.startNarrow[3] = (float)v.d.place[2];
+    v.wScaleNarrow = (float)v.start64.wScale;
+    v.stepBaseNarrow = (float)v.start64.stepBase;
     v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
     v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * frame64.spin[1]);
     v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);

@@ -91,8 +91,13 @@ int main() {
             RayConst<Op> cw;
             RayState<Op> sw, next;
             Op k1, a1[3];
-            g_ops = 0;
             rayStartWith(f, view, Op(0.1), Op(0.2), Op(0.0), cw, sw);
+            /* (the mixed trace's set-up in FP64: the constants of motion alone, and the step's terms in
+             * double; the first state and the step are its FP32 work) */
+            RayConst<Op> cm;
+            MotionFactors<Op> mf;
+            g_ops = 0;
+            motionConstants(f, view, Op(0.1), Op(0.2), cm, mf);
             const StepTerms<Op> terms = stepTerms(cw.step);
             printf("wide_start%s %ld\n", tag, g_ops);
             g_ops = 0;
