@@ -78,9 +78,13 @@ def config4_params():
     return target, start
 
 
-def config5_fits(count: int = 32, seed: int = 3, stars: float = 1.0):
+DRAWN = (0, 1, 2)  # the parameters configuration 5 draws: spin, inclination, inner radius
+
+
+def config5_fits(count: int = 32, seed: int = 3, stars: float = 1.0, offset=DRAWN):
     """Independent fits: targets a in [0.1, 0.99], i in [20, 85] deg, r_in in [1, 1.5] r_ISCO (q = 3 and
-    r_obs = 30 held), each start every parameter off by 15% up or down (the spin at most 0.997)."""
+    r_obs = 30 held), each start off by 15% up or down in the parameters `offset` (by default the three
+    drawn ones; the spin at most 0.997), the rest at the target's values."""
     rng = np.random.default_rng(seed)
     fits = []
     for _ in range(count):
@@ -89,7 +93,9 @@ def config5_fits(count: int = 32, seed: int = 3, stars: float = 1.0):
         scale = float(rng.uniform(1.0, 1.5))
         target = hole_params(a, incl, scale, 3.0, 30.0, seed=seed, stars=stars)
         signs = rng.choice([-1.0, 1.0], size=5)
-        start = theta_of(target) * (1.0 + 0.15 * signs)
+        start = theta_of(target)
+        for q in offset:
+            start[q] *= 1.0 + 0.15 * signs[q]
         start[0] = min(start[0], SPIN_LIMIT)
         fits.append((target, with_theta(target, start)))
     return fits
@@ -162,10 +168,18 @@ def project(theta: np.ndarray) -> np.ndarray:
     return t
 
 
-def fit_batch(adjoint: Adjoint, fits, steps: int = 200, lr: float = 1e-2):
+def _free_mask(free):
+    torch = _torch()
+    mask = torch.zeros(5, dtype=torch.float64)
+    mask[list(free)] = 1.0
+    return mask
+
+
+def fit_batch(adjoint: Adjoint, fits, steps: int = 200, lr: float = 1e-2, free=DRAWN):
     """Adam on every fit at once (lr on theta relative to its starting guess, so one rate suits every
-    parameter's scale); each step one adjoint launch over all views.  Returns the fitted theta (n, 5),
-    the per-step mean loss, and the wall time in seconds (targets excluded)."""
+    parameter's scale); each step one adjoint launch over all views.  Only the parameters `free` move
+    (by default the three configuration 5 draws); the others stay at their starting values.  Returns the
+    fitted theta (n, 5), the per-step mean loss, and the wall time in seconds (targets excluded)."""
     torch = _torch()
     HoleLoss = hole_loss()
     targets_p = [t for t, _ in fits]
@@ -173,6 +187,7 @@ def fit_batch(adjoint: Adjoint, fits, steps: int = 200, lr: float = 1e-2):
     targets = adjoint.render(targets_p)
     scale = torch.from_numpy(np.stack([theta_of(s) for s in base]))
     z = torch.zeros_like(scale, requires_grad=True)
+    mask = _free_mask(free)
     opt = torch.optim.Adam([z], lr=lr)
     history = []
     torch.cuda.synchronize()
@@ -183,6 +198,7 @@ def fit_batch(adjoint: Adjoint, fits, steps: int = 200, lr: float = 1e-2):
         total = loss.sum()
         opt.zero_grad()
         total.backward()
+        z.grad *= mask
         opt.step()
         with torch.no_grad():
             kept = torch.from_numpy(project((scale * (1.0 + z)).numpy()))
@@ -277,13 +293,15 @@ def fd_gradients(fp64: Fp64Loss, params, targets, h: float = 1e-4):
     return out[:, 0], grads
 
 
-def fit_batch_fd(fp64: Fp64Loss, fits, targets, steps: int = 200, lr: float = 1e-2, h: float = 1e-4):
+def fit_batch_fd(fp64: Fp64Loss, fits, targets, steps: int = 200, lr: float = 1e-2, h: float = 1e-4,
+                 free=DRAWN):
     """The same fit as fit_batch with gradients from fd_gradients (FP64 renders, central differences):
     the fitted theta (n, 5), the per-step mean loss, and the wall time in seconds."""
     torch = _torch()
     base = [s for _, s in fits]
     scale = torch.from_numpy(np.stack([theta_of(s) for s in base]))
     z = torch.zeros_like(scale, requires_grad=True)
+    mask = _free_mask(free)
     opt = torch.optim.Adam([z], lr=lr)
     history = []
     torch.cuda.synchronize()
@@ -292,7 +310,7 @@ def fit_batch_fd(fp64: Fp64Loss, fits, targets, steps: int = 200, lr: float = 1e
         theta = (scale * (1.0 + z)).detach().numpy()
         loss, grad = fd_gradients(fp64, [with_theta(b, t) for b, t in zip(base, theta)], targets, h)
         opt.zero_grad()
-        z.grad = torch.from_numpy(grad) * scale  # d loss / d z = d loss / d theta * scale
+        z.grad = torch.from_numpy(grad) * scale * mask  # d loss / d z = d loss / d theta * scale
         opt.step()
         with torch.no_grad():
             kept = torch.from_numpy(project((scale * (1.0 + z)).numpy()))

@@ -105,10 +105,16 @@ def test_fit_workloads():
         tt, ss = fit.theta_of(t), fit.theta_of(s)
         assert 0.1 <= tt[0] <= 0.99 and math.radians(20) <= tt[1] <= math.radians(85) and 1.0 <= tt[2] <= 1.5
         off = np.abs(ss / tt - 1.0)
-        assert np.all(np.abs(off[1:] - 0.15) < 1e-12)
+        # the drawn parameters start 15% off (the spin capped), the emissivity index and distance on target
+        assert np.all(np.abs(off[1:3] - 0.15) < 1e-12) and np.all(off[3:] == 0.0)
         assert ss[0] <= fit.SPIN_LIMIT
     again = fit.config5_fits()
     assert all(np.array_equal(fit.theta_of(a[1]), fit.theta_of(b[1])) for a, b in zip(fits, again))
+    every = fit.config5_fits(offset=range(5))
+    for (t, s), (t3, _) in zip(every, fits):
+        tt, ss = fit.theta_of(t), fit.theta_of(s)
+        assert np.array_equal(tt, fit.theta_of(t3))  # the same targets either way
+        assert np.all(np.abs(np.abs(ss / tt - 1.0)[1:] - 0.15) < 1e-12)
 
 
 def test_projection_keeps_scenes_valid():
