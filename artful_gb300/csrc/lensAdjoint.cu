@@ -45,6 +45,7 @@ struct alignas(16) AdjointView {
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int kMaxK = ARTF_CUDA_ADJOINT_MAX_CHECKPOINT;
 constexpr int kMaxSteps = 192;
 constexpr float kTurn = .15915494f; /* 1 / 2 pi, the reference's constant */
 
@@ -76,7 +77,8 @@ __device__ __forceinline__ void dragBack(float a, float xiA, float x, float dBar
 }
 
 /* The drag rate at x with the pieces its adjoint takes: the numerator, the reciprocal of the denominator
- * and whether the denominator was held at its floor.  One reciprocal serves the rate and its adjoint. */
+ * and whether the denominator was held at its floor.  One reciprocal serves the rate and its adjoint
+ * (four reciprocals a step fewer than dragAt and dragBack apart: 1.314 -> 1.293 ms for 8 views). */
 struct DragTerms {
     float rate, num, inv;
     bool held;
@@ -730,24 +732,12 @@ __device__ __forceinline__ void loadState(const float4* at, size_t stride, RaySt
     s.psi = c.x, s.drag = c.y, through = c.z;
 }
 
-/* The reverse kernel's segment rings.  A block holds one slot of a pool for its lifetime: a ring of
- * K + 1 states for each of its warps, each of three field planes across the warp's lanes.  The pool has a
- * slot for every block the GPU holds at once and later blocks reuse the slots, so the rings stay in L2
- * (rings of a thread's own, in local memory, had new addresses in every block and streamed to DRAM). */
-struct Rings {
-    float4* plane;      /* 3 planes of planeStride float4: (u, w, n0, n1), (n2, v0, v1, v2), (psi, drag, through, 0) */
-    unsigned* held;     /* a flag a slot: 1 while a block holds it (zeroed before each launch) */
-    size_t planeStride; /* slots * warps a block * depth * 32 */
-    int perSm, count, depth;
-};
-
 struct AdjointLaunch {
     const AdjointView* views;
     float* partials; /* 8 floats a tile: the loss, the five gradient components, two unused */
     unsigned long long* counters;
     const int* order; /* each view's tiles, heaviest first (tilesPerView a view), or NULL: in order */
     Trail trail;
-    Rings rings;
     int tilesX, tilesPerView, totalTiles, K;
 };
 
@@ -871,34 +861,17 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(con
     if ((threadIdx.x & 31) == 0) L.partials[t.tile * 8] = loss;
 }
 
-/* The ring slot a block holds for its lifetime: first among its SM's share of the pool, else anywhere in
- * it; -1 only if every slot is held, which the pool's size (a slot for each block the GPU can hold at
- * once) rules out.  No waiting: at most perSm + count attempts. */
-__device__ int claimRing(const Rings& r) {
-    unsigned sm;
-    asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
-    const int first = (int)(sm % (unsigned)(r.count / r.perSm)) * r.perSm;
-    for (int i = 0; i < r.perSm; ++i)
-        if (atomicCAS(r.held + first + i, 0u, 1u) == 0u) return first + i;
-    for (int i = 0; i < r.count; ++i)
-        if (atomicCAS(r.held + i, 0u, 1u) == 0u) return i;
-    return -1;
-}
-
-__device__ __forceinline__ void putRing(const Rings& r, size_t at, const RayState<float>& s, float through) {
-    r.plane[at] = make_float4(s.u, s.w, s.n[0], s.n[1]);
-    r.plane[at + r.planeStride] = make_float4(s.n[2], s.v[0], s.v[1], s.v[2]);
-    r.plane[at + 2 * r.planeStride] = make_float4(s.psi, s.drag, through, 0.f);
-}
-
-/* One tile's rays taken back: each ray's steps from its last contributing one, a segment at a time,
- * each segment recomputed from its kept state into the warp's ring of K + 1 states (the segment's and
- * the one after it), then the ray's set-up.  The next state back is loaded from the ring a step ahead. */
-template <int kK>
-__device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const AdjointView& v, const TileLane& t, int slot) {
+/* The reverse kernel: each ray's steps taken back from its last contributing one, a segment at a time,
+ * each segment recomputed from its kept state into a ring of K states, then the ray's set-up; the tile's
+ * gradient to its slot. */
+template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(const AdjointLaunch L) {
+    __shared__ AdjointView v;
+    copyView(L, v);
+    __syncthreads();
+    TileLane t;
+    if (!tileLane(L, v, t)) return;
     const int K = kK ? kK : L.K;
     const Trail& tr = L.trail;
-    const Rings& rg = L.rings;
     float grad[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     const int4 head = t.inside ? tr.head[t.ray] : make_int4(0, 0, 0, 0);
     const int steps = head.x, top = head.y;
@@ -913,9 +886,7 @@ __device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const Adjoin
         const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
         const float4 bar = tr.bar[t.ray];
         const float sumBar[3] = {bar.x, bar.y, bar.z}, throughEnd = bar.w;
-        const size_t ring = ((size_t)(slot * (kThreads / 32) + (int)(threadIdx.x >> 5)) * rg.depth) * 32 +
-                            (threadIdx.x & 31);
-        const size_t ps = rg.planeStride;
+        Kept ring[kK ? kK : kMaxK];
         StepBar next;
         memset(&next, 0, sizeof next);
         ConstBar g;
@@ -923,7 +894,7 @@ __device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const Adjoin
         float throughBar = 0.f;
         for (int first = ((top - 1) / K) * K; first >= 0; first -= K) {
             const int last = min(first + K, top); /* steps first .. last - 1 */
-            /* the segment's states from its kept start, then the state after its last step: the ray's end
+            /* the segment's states from its kept start; the state after its last step is the ray's end
              * when that step was the ray's last, else one more step on */
             RayState<float> r;
             float through;
@@ -931,7 +902,7 @@ __device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const Adjoin
             float junk[3] = {0.f, 0.f, 0.f};
             unsigned n = 0;
             for (int step = first; step < last; ++step) {
-                putRing(rg, ring + (size_t)(step - first) * 32, r, through);
+                ring[step - first] = Kept{r, through};
                 if (step == steps - 1) break;
                 StepOut<float> o;
                 stepOnce(v, rhoScale, c, r, o, through, junk, n);
@@ -942,18 +913,8 @@ __device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const Adjoin
                 float unused;
                 loadState(tr.end + t.ray, tr.rays, after, unused);
             }
-            float4 pa = rg.plane[ring + (size_t)(last - 1 - first) * 32];
-            float4 pb = rg.plane[ring + (size_t)(last - 1 - first) * 32 + ps];
-            float4 pc = rg.plane[ring + (size_t)(last - 1 - first) * 32 + 2 * ps];
             for (int step = last - 1; step >= first; --step) {
-                Kept k;
-                k.s.u = pa.x, k.s.w = pa.y, k.s.n[0] = pa.z, k.s.n[1] = pa.w;
-                k.s.n[2] = pb.x, k.s.v[0] = pb.y, k.s.v[1] = pb.z, k.s.v[2] = pb.w;
-                k.s.psi = pc.x, k.s.drag = pc.y, k.through = pc.z;
-                if (step > first) {
-                    const size_t at = ring + (size_t)(step - 1 - first) * 32;
-                    pa = rg.plane[at], pb = rg.plane[at + ps], pc = rg.plane[at + 2 * ps];
-                }
+                const Kept k = ring[step - first];
                 StepOut<float> o;
                 o.next = after;
                 o.k1 = bendAt(c, k.s.u);
@@ -986,27 +947,6 @@ __device__ __forceinline__ void reverseTile(const AdjointLaunch& L, const Adjoin
         float sum = grad[q];
         for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xFFFFFFFFu, sum, off);
         if (lane == 0) L.partials[t.tile * 8 + 1 + q] = sum;
-    }
-}
-
-/* The reverse kernel: a block claims a ring slot, its warps take their tiles back, and the slot is given
- * back once every warp is done.  A block that finds no slot (none can, with the pool sized as it is)
- * marks the launch's status word instead of tracing. */
-template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(const AdjointLaunch L) {
-    __shared__ AdjointView v;
-    __shared__ int slot;
-    copyView(L, v);
-    if (threadIdx.x == 0) slot = claimRing(L.rings);
-    __syncthreads();
-    TileLane t;
-    if (tileLane(L, v, t)) {
-        if (slot >= 0) reverseTile<kK>(L, v, t, slot);
-        else if ((threadIdx.x & 31) == 0) atomicExch(L.counters + CStatus, 1ull);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && slot >= 0) {
-        __threadfence();
-        atomicExch(L.rings.held + slot, 0u);
     }
 }
 
@@ -1122,25 +1062,8 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
     memcpy(slot, &v, sizeof v);
 }
 
-/* The ring pool: a slot for each block of the reverse kernel the GPU holds at once (the larger of its
- * two instantiations' occupancies, on the current device). */
-static void ringPool(int& perSm, int& count) {
-    int device = 0, sms = 0, fixed = 0, given = 0;
-    cudaGetDevice(&device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fixed, adjointReverse<32>, kThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&given, adjointReverse<0>, kThreads, 0);
-    perSm = max(max(fixed, given), 1);
-    count = perSm * max(sms, 1);
-}
-
-/* The order's scratch: class counts and cursors, the ring pool's flags (these three zeroed before each
- * launch), then the tiles' weights and order. */
 size_t adjointOrderBytes(int count, int width, int height) {
-    int perSm, slots;
-    ringPool(perSm, slots);
-    return sizeof(unsigned) * (2 * kClassStride * (size_t)count + (size_t)slots) +
-           sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
+    return sizeof(unsigned) * 2 * kClassStride * (size_t)count + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
 }
 
 /* The trail's rays: 32 a tile, padding lanes included. */
@@ -1148,18 +1071,12 @@ static size_t trailRays(int count, int width, int height) { return (size_t)count
 
 static int trailSegments(int K) { return (kMaxSteps + K - 1) / K; }
 
-/* Each ray's head, bar, end and kept states, then the ring pool's three planes. */
 size_t adjointTrailBytes(int count, int width, int height, int K) {
-    int perSm, slots;
-    ringPool(perSm, slots);
-    const size_t ringStates = (size_t)slots * (kThreads / 32) * (K + 1) * 32;
-    return trailRays(count, width, height) * sizeof(float4) * (2 + 3 + 3 * (size_t)trailSegments(K)) +
-           3 * ringStates * sizeof(float4);
+    return trailRays(count, width, height) * sizeof(float4) * (2 + 3 + 3 * (size_t)trailSegments(K));
 }
 
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
                           float* partials, double* results, cudaStream_t stream, void* orderScratch, void* trail) {
-    if (!orderScratch) return cudaErrorInvalidValue; /* (it holds the ring pool's flags) */
     AdjointLaunch L;
     L.views = (const AdjointView*)table;
     L.partials = partials;
@@ -1174,25 +1091,18 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.trail.bar = (float4*)(L.trail.head + L.trail.rays);
     L.trail.end = L.trail.bar + L.trail.rays;
     L.trail.saved = L.trail.end + 3 * L.trail.rays;
-    int perSm, slots;
-    ringPool(perSm, slots);
-    L.rings.perSm = perSm;
-    L.rings.count = slots;
-    L.rings.depth = K + 1;
-    L.rings.planeStride = (size_t)slots * (kThreads / 32) * (K + 1) * 32;
-    L.rings.plane = L.trail.saved + 3 * (size_t)trailSegments(K) * L.trail.rays;
-    unsigned* classes = (unsigned*)orderScratch;
-    unsigned* cursors = classes + kClassStride * (size_t)count;
-    L.rings.held = cursors + kClassStride * (size_t)count;
-    int* weights = (int*)(L.rings.held + slots);
-    int* order = weights + (size_t)count * L.tilesPerView;
-    const cudaError_t e =
-        cudaMemsetAsync(orderScratch, 0, sizeof(unsigned) * (2 * kClassStride * (size_t)count + slots), stream);
-    if (e != cudaSuccess) return e;
-    const dim3 probeGrid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
-    adjointProbe<<<probeGrid, 128, 0, stream>>>(L, weights, classes);
-    adjointPlace<<<probeGrid, 128, 0, stream>>>(L, weights, classes, cursors, order);
-    L.order = order;
+    if (orderScratch) {
+        unsigned* classes = (unsigned*)orderScratch;
+        unsigned* cursors = classes + kClassStride * (size_t)count;
+        int* weights = (int*)(cursors + kClassStride * (size_t)count);
+        int* order = weights + (size_t)count * L.tilesPerView;
+        const cudaError_t e = cudaMemsetAsync(orderScratch, 0, sizeof(unsigned) * 2 * kClassStride * (size_t)count, stream);
+        if (e != cudaSuccess) return e;
+        const dim3 grid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
+        adjointProbe<<<grid, 128, 0, stream>>>(L, weights, classes);
+        adjointPlace<<<grid, 128, 0, stream>>>(L, weights, classes, cursors, order);
+        L.order = order;
+    }
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
     const dim3 grid(blocks, (unsigned)count);
     if (K == 32) {

@@ -772,7 +772,7 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.wScaleNarrow = (float)v.start64.wScale;
     v.stepBaseNarrow = (float)v.start64.stepBase;
     v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
-    v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .8f) * frame64.spin[1]);
+    v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .95f) * frame64.spin[1]);
     v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);
     v.share = l.jitter ? 1.f / (float)l.jitter : frame.image[3];
     v.jitter = l.jitter;

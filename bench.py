@@ -203,9 +203,9 @@ def sweep(args):
                       "vs_fp64_half": endpoint_error(e32, e64h, img32, img64h)}), flush=True)
     G = capi
     variants = [
-        ("defaults: all guards, band 0.8, batch 32, refill 32, wait 256, block 128", dict()),
-        ("band 0.5", dict(band=0.5)),
-        ("band 0.9", dict(band=0.9)),
+        ("defaults: all guards, band 0.95, batch 32, refill 32, wait 256, block 128", dict()),
+        ("band 0.8", dict(band=0.8)),
+        ("band 0.99", dict(band=0.99)),
         ("batch 16", dict(batch=16)),
         ("batch 24", dict(batch=24)),
         ("refill 8", dict(refill=8)),
@@ -601,6 +601,8 @@ def main():
         "mixed_over_fp64": side["fp64"]["ms_per_frame"] / ms_mixed,
         "steps_per_s": s_mixed.steps / (ms_mixed * 1e-3) * world,
         "fp64_step_share": s_mixed.fp64Steps / max(1, s_mixed.steps),
+        "fp64_substeps": {"horizon_band": s_mixed.fp64Horizon, "radial_turn": s_mixed.fp64Radial,
+                          "polar_turn": s_mixed.fp64Polar, "warp_rounds": s_mixed.fp64Rounds},
         "side": side,
         "endpoint_error": endpoint,
         "roofline": {"bound": "fp64", "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",

@@ -189,7 +189,7 @@ typedef struct ArtfCudaTraceOptions {
     float stepScale;     /* 1: the reference's step (pi/24 / sqrt(max(K, 4))); 0.5: half steps, with twice
                           * the step cap. 0 means 1 */
     float horizonBand;   /* mixed: FP64 radial sub-steps where u > band * (0.995 / r+), i.e. within about
-                          * r+ / band of the hole; 0 means the default 0.8 */
+                          * r+ / band of the hole; 0 means the default 0.95 */
     int blockSize;       /* threads a block: 0 picks the tuned value */
     int compactEvery;    /* steps between warp refills: 0 picks the tuned value */
     int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */

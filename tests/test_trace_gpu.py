@@ -167,7 +167,7 @@ def test_mixed_guards_select_their_fp64_work(lib, ctx):
     assert s.fp64Radial == 0 and s.fp64Polar == 0 and s.fp64Horizon > 0
     _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, guards=capi.GUARD_POLAR | capi.GUARD_MOTION)
     assert s.fp64Radial == 0 and s.fp64Horizon == 0 and s.fp64Polar > 0
-    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, band=0.9)
+    _, s = g.trace(lib, ctx, frame, frame64, capi.MIXED, band=0.99)
     assert s.fp64Horizon < s_all.fp64Horizon
 
 
