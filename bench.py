@@ -77,6 +77,12 @@ def parse():
     return p.parse_args()
 
 
+def scale_of(p):
+    """A parameter point's scale for finite-difference steps: each parameter's size, at least 0.1."""
+    from artful_gb300 import fit
+    return np.array([max(abs(x), 1e-1) for x in fit.theta_of(p)])
+
+
 def gradient_bias(args):
     """Why the inverse fits do not recover their parameters.  On the first fits of the configuration-5
     workload (256 x 144, targets from seed 3, starts 15% off): the adjoint's gradient against central
@@ -97,9 +103,6 @@ def gradient_bias(args):
     adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
     targets = adj.render([t for t, _ in fits])
     fp64 = fit.Fp64Loss(lib, ctx, w, h, m, lib.artfCudaDeviceFluid(ctx), 10 * len(fits))
-
-    def scale_of(p):
-        return np.array([max(abs(x), 1e-1) for x in fit.theta_of(p)])
 
     def differences(params, step):
         """Central differences of the FP64 loss, each parameter moved by step times its size."""
@@ -155,8 +158,69 @@ def gradient_bias(args):
         alone[name] = row
     print(json.dumps({"gradient_bias": table, "fits": len(fits),
                       "loss_start_to_target_median": line, "loss_alone_offsets": list(offsets),
-                      "loss_alone_median": alone}), flush=True)
+                      "loss_alone_median": alone, "pixels": pixel_decomposition(adj, fits, targets)}),
+          flush=True)
     lib.artfCudaDestroy(ctx)
+
+
+def pixel_decomposition(adj, fits, targets, step=1e-3, fine=1e-4):
+    """Where the adjoint's gradient and the finite differences part, pixel by pixel, at the fits' starts.
+    Each pixel's loss (its squared RGB error over 3 x pixels) by the adjoint's own forward renders (FP32,
+    the function the adjoint differentiates) at theta +- step and theta +- fine (each times the
+    parameter's size).  A pixel is *smooth* in a parameter when its two
+    central differences agree within 5 % (the loss is differentiable there at the step's scale), else
+    it is *rough*: an edge, a truncated colour or ring row, a class change or a star's tent crossed
+    within the step.  Per parameter: the central-difference gradient at `step` summed over all pixels,
+    and the share of it on the rough pixels; the adjoint's sum (its per-pixel gradients) over all and
+    over the smooth pixels, against the fine differences on the smooth pixels; how many pixels are
+    rough."""
+    import torch
+    from artful_gb300 import fit
+    n = len(fits)
+    start = [s for _, s in fits]
+    h, w = adj.height, adj.width
+    grads = torch.zeros((n, h, w, 5), dtype=torch.float32, device="cuda")
+    adj(start, targets, pixel_grads=grads)
+    grads = grads.double().cpu().numpy()
+
+    def pixel_losses(params):
+        """Each pixel's loss, rendered by the adjoint's own forward pass (the function it differentiates)."""
+        out = []
+        for lo in range(0, len(params), n):
+            chunk = params[lo:lo + n]
+            d = adj.render(chunk)[..., :3].double() - targets[:len(chunk), ..., :3].double()
+            out.append(((d * d).sum(-1) / (3 * h * w)).cpu().numpy())
+        return np.concatenate(out)
+
+    def central(q, size):
+        moved = []
+        for sign in (1.0, -1.0):
+            for p in start:
+                th = fit.theta_of(p)
+                th[q] += sign * size * scale_of(p)[q]
+                moved.append(fit.with_theta(p, th))
+        lm = pixel_losses(moved)
+        sc = np.array([size * scale_of(p)[q] for p in start])[:, None, None]
+        return (lm[:n] - lm[n:]) / (2 * sc)
+
+    rows = {}
+    for q, name in enumerate(fit.PARAM_NAMES):
+        coarse, near = central(q, step), central(q, fine)
+        floor = 1e-6 * np.abs(near).max()
+        smooth = np.abs(coarse - near) <= 0.05 * np.abs(near) + floor
+        g = grads[..., q]
+        rows[name] = {
+            "fd_all": float(coarse.sum() / n), "fd_share_on_rough_pixels":
+                float(np.abs(coarse[~smooth]).sum() / max(np.abs(coarse).sum(), 1e-30)),
+            "adjoint_all": float(g.sum() / n), "adjoint_over_fd_all": float(g.sum() / coarse.sum()),
+            "adjoint_over_fine_fd_smooth": float(g[smooth].sum() / near[smooth].sum())
+            if abs(near[smooth].sum()) > 1e-30 else None,
+            "smooth_pixels_within_2pct": float(np.mean(np.abs(g - near)[smooth] <= 0.02 * np.abs(near)[smooth] + floor)),
+            "smooth_cosine": float(np.dot(g[smooth], near[smooth]) /
+                                   (np.linalg.norm(g[smooth]) * np.linalg.norm(near[smooth]) + 1e-30)),
+            "smooth_l1_error": float(np.abs(g - near)[smooth].sum() / max(np.abs(near)[smooth].sum(), 1e-30)),
+            "rough_pixels": float(1.0 - smooth.mean())}
+    return {"step": step, "fine": fine, "per_parameter": rows}
 
 
 def sweep(args):
@@ -780,6 +844,10 @@ def fit_measurement(lib, ctx, fd_fits):
                        "(q = 3, r_obs = 30 held), 200 Adam steps, lr 1e-2 (relative to the start), adjoint K=32",
            "wall_s": wall, "wall_per_fit_s": wall / len(fits), "start_error": 0.15,
            "loss_first_last": [float(history[0]), float(history[-1])], "recovery_error": summary(err)}
+    # why: the adjoint's gradient against finite differences of its own forward renders, pixel by pixel,
+    # at the first six fits' starts (the share of the gradient on pixels where the loss is not smooth)
+    six = adj.render([t for t, _ in fits[:6]])
+    out["gradient_decomposition"] = pixel_decomposition(adj, fits[:6], six)
     all5 = fit.config5_fits(32, seed=3, offset=range(5))
     theta5, history5, wall5 = fit.fit_batch(adj, all5, steps=200, lr=1e-2, free=range(5))
     out["five_parameters"] = {"workload": "the same fits with all five parameters started 15% off and fitted",
