@@ -1018,21 +1018,46 @@ __global__ void __launch_bounds__(128) adjointPlace(const AdjointLaunch L, const
     if (active) order[(size_t)blockIdx.y * L.tilesPerView + runs[w] + within] = local;
 }
 
-/* One block a view: its tiles' sums added in double, in a fixed order. */
-__global__ void __launch_bounds__(256) adjointSums(const float* partials, int tilesPerView, double* results) {
-    __shared__ double part[256];
-    const float* mine = partials + (size_t)blockIdx.x * tilesPerView * 8;
-    for (int k = 0; k < 6; ++k) {
-        double s = 0.0;
-        for (int b = threadIdx.x; b < tilesPerView; b += 256) s += (double)mine[(size_t)b * 8 + k];
-        part[threadIdx.x] = s;
+/* A view's tiles' sums in double, in a fixed order whatever the scheduling: each of kSumBlocks blocks
+ * takes a run of the view's tiles (thread t adds the run's tiles t, t + 256, ... in turn, then a tree over
+ * the threads, the six sums of a tile read together), and the view's last block to finish (a ticket a
+ * view, zeroed before the launch) adds the blocks' sums in block order. */
+constexpr int kSumBlocks = 64;
+
+__global__ void __launch_bounds__(256) adjointSums(const float* partials, int tilesPerView, double* blockSums,
+                                                   unsigned* tickets, double* results) {
+    __shared__ double part[6][256];
+    __shared__ unsigned ticket;
+    const int view = (int)blockIdx.y, run = (tilesPerView + kSumBlocks - 1) / kSumBlocks;
+    const int begin = (int)blockIdx.x * run, end = min(begin + run, tilesPerView);
+    const float4* mine = reinterpret_cast<const float4*>(partials + (size_t)view * tilesPerView * 8);
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = begin + (int)threadIdx.x; b < end; b += 256) {
+        const float4 lo = mine[(size_t)b * 2], hi = mine[(size_t)b * 2 + 1];
+        s[0] += (double)lo.x, s[1] += (double)lo.y, s[2] += (double)lo.z, s[3] += (double)lo.w;
+        s[4] += (double)hi.x, s[5] += (double)hi.y;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) part[k][threadIdx.x] = s[k];
+    __syncthreads();
+    for (int width = 128; width > 0; width >>= 1) {
+        if ((int)threadIdx.x < width)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + width];
         __syncthreads();
-        for (int width = 128; width > 0; width >>= 1) {
-            if ((int)threadIdx.x < width) part[threadIdx.x] += part[threadIdx.x + width];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) results[(size_t)blockIdx.x * 8 + k] = part[0];
-        __syncthreads();
+    }
+    double* sums = blockSums + (size_t)view * kSumBlocks * 8;
+    if (threadIdx.x < 6) sums[blockIdx.x * 8 + threadIdx.x] = part[threadIdx.x][0];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) ticket = atomicAdd(tickets + view, 1u);
+    __syncthreads();
+    if (ticket != kSumBlocks - 1) return;
+    __threadfence();
+    if (threadIdx.x < 6) {
+        double total = 0.0;
+        for (int b = 0; b < kSumBlocks; ++b) total += __ldcg(sums + b * 8 + threadIdx.x);
+        results[(size_t)view * 8 + threadIdx.x] = total;
     }
 }
 
@@ -1062,8 +1087,13 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
     memcpy(slot, &v, sizeof v);
 }
 
+/* The order's scratch: class counts, cursors and the sums' tickets (zeroed before each launch), the
+ * tiles' weights and order, then the sums' blocks (doubles). */
+static size_t orderHead(int count) { return sizeof(unsigned) * (2 * kClassStride + 1) * (size_t)count; }
+
 size_t adjointOrderBytes(int count, int width, int height) {
-    return sizeof(unsigned) * 2 * kClassStride * (size_t)count + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
+    const size_t ints = orderHead(count) + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
+    return (ints + 15) / 16 * 16 + sizeof(double) * 8 * kSumBlocks * (size_t)count;
 }
 
 /* The trail's rays: 32 a tile, padding lanes included. */
@@ -1091,18 +1121,20 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.trail.bar = (float4*)(L.trail.head + L.trail.rays);
     L.trail.end = L.trail.bar + L.trail.rays;
     L.trail.saved = L.trail.end + 3 * L.trail.rays;
-    if (orderScratch) {
-        unsigned* classes = (unsigned*)orderScratch;
-        unsigned* cursors = classes + kClassStride * (size_t)count;
-        int* weights = (int*)(cursors + kClassStride * (size_t)count);
-        int* order = weights + (size_t)count * L.tilesPerView;
-        const cudaError_t e = cudaMemsetAsync(orderScratch, 0, sizeof(unsigned) * 2 * kClassStride * (size_t)count, stream);
-        if (e != cudaSuccess) return e;
-        const dim3 grid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
-        adjointProbe<<<grid, 128, 0, stream>>>(L, weights, classes);
-        adjointPlace<<<grid, 128, 0, stream>>>(L, weights, classes, cursors, order);
-        L.order = order;
-    }
+    if (!orderScratch) return cudaErrorInvalidValue; /* (it holds the sums' tickets and blocks too) */
+    unsigned* classes = (unsigned*)orderScratch;
+    unsigned* cursors = classes + kClassStride * (size_t)count;
+    unsigned* tickets = cursors + kClassStride * (size_t)count;
+    int* weights = (int*)(tickets + count);
+    int* order = weights + (size_t)count * L.tilesPerView;
+    const size_t ints = orderHead(count) + sizeof(int) * 2 * (size_t)count * L.tilesPerView;
+    double* blockSums = (double*)((char*)orderScratch + (ints + 15) / 16 * 16);
+    const cudaError_t e = cudaMemsetAsync(orderScratch, 0, orderHead(count), stream);
+    if (e != cudaSuccess) return e;
+    const dim3 probeGrid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
+    adjointProbe<<<probeGrid, 128, 0, stream>>>(L, weights, classes);
+    adjointPlace<<<probeGrid, 128, 0, stream>>>(L, weights, classes, cursors, order);
+    L.order = order;
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
     const dim3 grid(blocks, (unsigned)count);
     if (K == 32) {
@@ -1112,7 +1144,8 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
         adjointForward<0><<<grid, kThreads, 0, stream>>>(L);
         adjointReverse<0><<<grid, kThreads, 0, stream>>>(L);
     }
-    adjointSums<<<count, 256, 0, stream>>>(partials, L.tilesPerView, results);
+    adjointSums<<<dim3(kSumBlocks, (unsigned)count), 256, 0, stream>>>(partials, L.tilesPerView, blockSums, tickets,
+                                                                      results);
     return cudaGetLastError();
 }
 

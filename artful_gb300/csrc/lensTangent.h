@@ -37,7 +37,8 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
                           float* partials, double* results, cudaStream_t stream, void* orderScratch, void* trail);
 size_t adjointTrailBytes(int count, int width, int height, int K);
-/* Device bytes of the adjoint's heavy-first tile order (orderScratch above; NULL: the tiles in order). */
+/* Device bytes of the adjoint's order scratch (orderScratch above, required): the heavy-first tile order
+ * and the gradient sums' blocks and tickets. */
 size_t adjointOrderBytes(int count, int width, int height);
 
 }  // namespace artf
