@@ -587,6 +587,34 @@ def main():
                       "steps_per_s": s.steps / (ms * 1e-3), "flops_per_frame": s.flops}
     side["fp64"]["flops_per_frame"] = stats_of(capi.FP64).flops
 
+    # the same view with the reference's own 2 x 2 stratified rays a pixel (the frame's samples, no
+    # jitter), through the same public call: mixed and the exact FP32 trace (the reference's bits)
+    strat_scene = scenes.Scene("c2_2x2", scenes.hole_desc(0.998, samples=2), scenes.camera(85.0, 50.0), w, h,
+                               seed=scene.seed, emissivity=scene.emissivity)
+    strat_frame = scenes.frame(strat_scene)[0]
+
+    def timed_strat(precision, steps):
+        o = capi.TraceOptions(precision, 0, 0, 1.0, 0.0, 0, 0, 1)
+        with torch.cuda.stream(stream):
+            capi.check(lib.artfCudaHoleTrace(ctx, C.byref(strat_frame), None, None, None, C.byref(o),
+                                             hdr.data_ptr(), None, None))
+            total = 0.0
+            for _ in range(steps):
+                flush.fill_(1)
+                start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                start.record(stream)
+                capi.check(lib.artfCudaHoleTrace(ctx, C.byref(strat_frame), None, None, None, C.byref(o),
+                                                 hdr.data_ptr(), None, None))
+                stop.record(stream)
+                stop.synchronize()
+                total += start.elapsed_time(stop)
+        return total / steps
+
+    stratified = {}
+    for name, prec in (("mixed", capi.MIXED), ("fp32_exact", capi.EXACT)):
+        ms = timed_strat(prec, args.steps)
+        stratified[name] = {"ms_per_frame": ms, "geodesics_per_s": geodesics / (ms * 1e-3)}
+
     # endpoint error of the mixed trace: against FP64 at the same step (precision) and at half step
     # (precision and discretisation), over every ray of the frame
     def ends_of(precision, step_scale=1.0):
@@ -668,6 +696,7 @@ def main():
         "fp64_substeps": {"horizon_band": s_mixed.fp64Horizon, "radial_turn": s_mixed.fp64Radial,
                           "polar_turn": s_mixed.fp64Polar, "warp_rounds": s_mixed.fp64Rounds},
         "side": side,
+        "stratified_2x2": stratified,
         "endpoint_error": endpoint,
         "roofline": {"bound": "fp64", "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
                      "frac": achieved64 / peak64, "traffic": traffic,
