@@ -103,24 +103,6 @@ __device__ __forceinline__ void dragBackWith(float a, float xiA, float x, const 
     g.xiA += numBar * a * x * x;
 }
 
-/* n'' = A(n) = (-c nx, -c ny, a^2 nz - c nz), c = K + 2 a^2 nz^2. */
-__device__ __forceinline__ void accelOf(float a, float big, const float* n, float* out) {
-    const float c = big + 2.f * a * a * (n[2] * n[2]);
-    out[0] = -c * n[0], out[1] = -c * n[1], out[2] = a * a * n[2] - c * n[2];
-}
-
-/* A(n) taken back from its adjoint. */
-__device__ __forceinline__ void accelBack(float a, float big, const float* n, const float* outBar, float* nBar,
-                                          ConstBar& g) {
-    const float a2 = a * a, c = big + 2.f * a2 * (n[2] * n[2]);
-    const float cBar = -(n[0] * outBar[0] + n[1] * outBar[1] + n[2] * outBar[2]);
-    nBar[0] += -c * outBar[0];
-    nBar[1] += -c * outBar[1];
-    nBar[2] += (a2 - c) * outBar[2] + cBar * 4.f * a2 * n[2];
-    g.a += 2.f * a * n[2] * outBar[2] + cBar * 4.f * a * n[2] * n[2];
-    g.big += cBar;
-}
-
 /* lens.inc:30-41's polynomial arctangent (in turns): its slopes in y and x. */
 __device__ __forceinline__ void turnsSlope(float y, float x, float& dy, float& dx) {
     const float ax = fabsf(x), ay = fabsf(y);
@@ -169,18 +151,51 @@ __device__ __forceinline__ void speedSlopes(const Frame<float>& f, int32_t row, 
 
 /* ---- the Nystrom step taken back (lens.inc:165-192) ------------------------------------------------ */
 
+/* What every step of a ray taken back takes from the ray alone, formed once a ray: the step's products
+ * (as stepTerms forms them) and the spin's. */
+struct BackTerms {
+    float h, half, eighth, halfSq, sixthSq, sixth, a, a2, twoA2, fourA2, fourA, twoA;
+};
+
+__device__ __forceinline__ BackTerms backTerms(float a, float step) {
+    BackTerms t;
+    const StepTerms<float> st = stepTerms(step);
+    t.h = step, t.half = st.half, t.eighth = st.eighth, t.halfSq = st.halfSquare, t.sixthSq = st.sixthSquare;
+    t.sixth = st.sixth;
+    t.a = a, t.a2 = a * a, t.twoA2 = 2.f * t.a2, t.fourA2 = 4.f * t.a2, t.fourA = 4.f * a, t.twoA = 2.f * a;
+    return t;
+}
+
+/* A(x) = (-c x0, -c x1, a^2 x2 - c x2), c = K + 2 a^2 x2^2 as the forward step forms it; returns c. */
+__device__ __forceinline__ float accelWith(const BackTerms& t, float big, const float* x, float* out) {
+    const float cc = big + t.twoA2 * (x[2] * x[2]);
+    out[0] = 0.f - cc * x[0], out[1] = 0.f - cc * x[1], out[2] = t.a2 * x[2] - cc * x[2];
+    return cc;
+}
+
+/* A(x) taken back from its adjoint y, with its c. */
+__device__ __forceinline__ void accelBackWith(const BackTerms& t, float cc, const float* x, const float* y, float* xBar,
+                                              ConstBar& g) {
+    const float cBar = -(x[0] * y[0] + x[1] * y[1] + x[2] * y[2]);
+    xBar[0] += -cc * y[0];
+    xBar[1] += -cc * y[1];
+    xBar[2] += (t.a2 - cc) * y[2] + cBar * t.fourA2 * x[2];
+    g.a += x[2] * (t.twoA * y[2] + cBar * t.fourA * x[2]);
+    g.big += cBar;
+}
+
 /* The polar part: from the adjoints of (n', v') and of the first stage's a1 (which a crossing reads), adds
  * to those of (n, v) and the constants. */
-__device__ void polarBack(float a, const RayConst<float>& c, const float* n, const float* v, const float* nNextBar,
-                          const float* vNextBar, const float* a1Extra, float* nBar, float* vBar, ConstBar& g) {
-    const float h = c.step, h2 = h * h, half = h * .5f, eighth = h2 * .125f, halfSq = h2 * .5f;
-    const float sixthSq = h2 * (1.f / 6.f), sixth = h * (1.f / 6.f);
+__device__ __forceinline__ void polarBack(const BackTerms& t, float big, const float* n, const float* v,
+                                          const float* nNextBar, const float* vNextBar, const float* a1Extra,
+                                          float* nBar, float* vBar, ConstBar& g) {
+    const float h = t.h, half = t.half, eighth = t.eighth, halfSq = t.halfSq, sixthSq = t.sixthSq, sixth = t.sixth;
     float a1[3], midN[3], a2s[3], endN[3], a3[3];
-    accelOf(a, c.big, n, a1);
+    const float c1 = accelWith(t, big, n, a1);
     for (int k = 0; k < 3; ++k) midN[k] = n[k] + half * v[k] + eighth * a1[k];
-    accelOf(a, c.big, midN, a2s);
+    const float c2 = accelWith(t, big, midN, a2s);
     for (int k = 0; k < 3; ++k) endN[k] = n[k] + h * v[k] + halfSq * a2s[k];
-    accelOf(a, c.big, endN, a3);
+    const float c3 = accelWith(t, big, endN, a3);
     float a1Bar[3], a2Bar[3], a3Bar[3], midBar[3] = {0.f, 0.f, 0.f}, endBar[3] = {0.f, 0.f, 0.f}, hBar = 0.f;
     for (int k = 0; k < 3; ++k) {
         /* n' = n + h v + h^2/6 (a1 + 2 a2);  v' = v + h/6 (a1 + a3 + 4 a2) */
@@ -192,47 +207,47 @@ __device__ void polarBack(float a, const RayConst<float>& c, const float* n, con
         hBar += nNextBar[k] * (v[k] + h * (a1[k] + 2.f * a2s[k]) * (1.f / 3.f)) +
                 vNextBar[k] * (a1[k] + a3[k] + 4.f * a2s[k]) * (1.f / 6.f);
     }
-    accelBack(a, c.big, endN, a3Bar, endBar, g);
+    accelBackWith(t, c3, endN, a3Bar, endBar, g);
     for (int k = 0; k < 3; ++k) { /* endN = n + h v + h^2/2 a2 */
         nBar[k] += endBar[k];
         vBar[k] += h * endBar[k];
         a2Bar[k] += halfSq * endBar[k];
         hBar += endBar[k] * (v[k] + h * a2s[k]);
     }
-    accelBack(a, c.big, midN, a2Bar, midBar, g);
+    accelBackWith(t, c2, midN, a2Bar, midBar, g);
     for (int k = 0; k < 3; ++k) { /* midN = n + h/2 v + h^2/8 a1 */
         nBar[k] += midBar[k];
         vBar[k] += half * midBar[k];
         a1Bar[k] += eighth * midBar[k];
         hBar += midBar[k] * (.5f * v[k] + .25f * h * a1[k]);
     }
-    accelBack(a, c.big, n, a1Bar, nBar, g);
+    accelBackWith(t, c1, n, a1Bar, nBar, g);
     g.step += hBar;
 }
 
 /* The radial part: from the adjoints of (u', w', psi', drag') and of k1, adds to those of (u, w, psi,
  * drag) and the constants. */
-__device__ void radialBack(float a, const RayConst<float>& c, float u, float w, float drag, float uNextBar,
-                           float wNextBar, float psiNextBar, float dragNextBar, float k1Extra, float& uBar, float& wBar,
-                           float& psiBar, float& dragBar, ConstBar& g) {
-    const float h = c.step, h2 = h * h, half = h * .5f, eighth = h2 * .125f, halfSq = h2 * .5f;
-    const float sixthSq = h2 * (1.f / 6.f), sixth = h * (1.f / 6.f);
+__device__ __forceinline__ void radialBack(const BackTerms& t, const RayConst<float>& c, float u, float w, float drag,
+                                           float uNextBar, float wNextBar, float psiNextBar, float dragNextBar,
+                                           float k1Extra, float& uBar, float& wBar, float& psiBar, float& dragBar,
+                                           ConstBar& g) {
+    const float h = t.h, half = t.half, eighth = t.eighth, halfSq = t.halfSq, sixthSq = t.sixthSq, sixth = t.sixth;
     const float k1 = bendAt(c, u);
     const float midU = u + half * w + eighth * k1;
     const float k2 = bendAt(c, midU);
     const float endU = u + h * w + halfSq * k2;
     const float k3 = bendAt(c, endU);
     float hBar = 0.f, midBar = 0.f;
-    if (a != 0.f) {
+    if (t.a != 0.f) {
         /* drag' = drag(u');  psi' = psi + h/6 (drag + drag' + 4 drag(midU)) */
         const float uNext = u + h * w + sixthSq * (k1 + (k2 + k2));
-        const DragTerms dNext = dragTerms(a, a * a, c.xiA, uNext), dMid = dragTerms(a, a * a, c.xiA, midU);
-        const float t = psiNextBar * sixth;
+        const DragTerms dNext = dragTerms(t.a, t.a2, c.xiA, uNext), dMid = dragTerms(t.a, t.a2, c.xiA, midU);
+        const float s6 = psiNextBar * sixth;
         psiBar += psiNextBar;
-        dragBar += t;
+        dragBar += s6;
         hBar += psiNextBar * (drag + dNext.rate + 4.f * dMid.rate) * (1.f / 6.f);
-        dragBackWith(a, c.xiA, midU, dMid, 4.f * t, midBar, g);
-        dragBackWith(a, c.xiA, uNext, dNext, dragNextBar + t, uNextBar, g);
+        dragBackWith(t.a, c.xiA, midU, dMid, 4.f * s6, midBar, g);
+        dragBackWith(t.a, c.xiA, uNext, dNext, dragNextBar + s6, uNextBar, g);
     }
     /* u' = u + h w + h^2/6 (k1 + 2 k2);  w' = w + h/6 (k1 + k3 + 4 k2) */
     uBar += uNextBar;
@@ -886,6 +901,7 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
         const float rhoScale = recipR(1.f - divR(f.inner, f.outer));
         const float4 bar = tr.bar[t.ray];
         const float sumBar[3] = {bar.x, bar.y, bar.z}, throughEnd = bar.w;
+        const BackTerms bt = backTerms(a, c.step);
         Kept ring[kK ? kK : kMaxK];
         StepBar next;
         memset(&next, 0, sizeof next);
@@ -918,7 +934,7 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
                 StepOut<float> o;
                 o.next = after;
                 o.k1 = bendAt(c, k.s.u);
-                accelOf(a, c.big, k.s.n, o.a1);
+                accelWith(bt, c.big, k.s.n, o.a1);
                 StepBar b;
                 memset(&b, 0, sizeof b);
                 b.nextU = next.u;
@@ -930,9 +946,9 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
                 Crossing<float> x;
                 if (crossingOf(f, rhoScale, c, k.s, o, x))
                     crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
-                radialBack(a, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w,
+                radialBack(bt, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w,
                            b.psi, b.drag, g);
-                polarBack(a, c, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
+                polarBack(bt, c.big, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
                 next = b;
                 after = k.s;
             }
