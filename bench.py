@@ -672,7 +672,7 @@ def main():
 
     cpu = None
     batch = None
-    adjoint = fitting = next_rows = None
+    adjoint = fitting = next_rows = whole_frame = None
     if rank == 0 and not args.quick:
         cpu = cpu_baseline(frame, map_, fluid, rays, scene.jitter_seed)
         versus_cpu = vs_reference_cpu(frame, map_, fluid, img_mixed, rays, scene.jitter_seed)
@@ -680,6 +680,7 @@ def main():
         adjoint = adjoint_measurement(lib, ctx, args.steps, flush)
         fitting = fit_measurement(lib, ctx, args.fd_fits)
         next_rows = next_rows_measurement(lib, ctx)
+        whole_frame = reference_frame_measurement(lib)
 
     lib.artfCudaDestroy(ctx)
     if rank != 0:
@@ -723,6 +724,8 @@ def main():
         line["inverse_fit"] = fitting
     if next_rows:
         line["disc_inputs"] = next_rows
+    if whole_frame:
+        line["reference_frame"] = whole_frame
     print(json.dumps(line), flush=True)
 
 
@@ -843,6 +846,75 @@ def next_rows_measurement(lib, ctx):
             "fluid_step_ms": steps[1], "fluid_step_ms_in_48": steps[48],
             "cpu_baseline": {"paint_disc_ms": oracle_paint_ms, "fluid_step_ms": oracle_step_ms, "cores": 1,
                              "kind": "port", "sample": "one painted map; 48 fluid steps"}}
+
+
+def reference_frame_measurement(lib, frames=30, warm=5):
+    """The reference's own published frame (its README's `blackhole` figure: 1920 x 1080, one ray a pixel,
+    a fluid step and bloom; 23 ms on a Vega 8 in Vulkan, 141 ms in its software renderer on a 4-core Ryzen
+    3200G), drawn through this backend's eight-entry table with device inputs: the reference's own scene (its
+    painted disc and its gas, made and stepped on the GPU), the exact trace (the reference's bits), bloom,
+    tone map and dither, the BGRA frame read back to the host every frame.  The hole's clock moves one gas
+    step (0.2) a frame.  Beside it the oracle port of the same frame's parts on the host cores."""
+    from artful_gb300 import capi, scenes
+    from oracle import binding
+    w, h = 1920, 1080
+    opts = capi.RendererOptions(4)
+    opts.width, opts.height = w, h
+    r = lib.artfCudaNew(C.byref(opts))
+    if not r:
+        raise RuntimeError(lib.artfCudaLastError())
+    vt = C.cast(r, C.POINTER(capi.RendererHead)).contents.vt.contents
+    lib.artfCudaRendererSetDeviceInputs(r, True)
+    scene = lib.artfCudaSceneNew()
+    cam = scenes.camera(80.0, 30.0)
+    lib.artfCudaSceneSetCamera(scene, C.byref(cam))
+    bgra = np.zeros((h, w), np.uint32)
+
+    def desc_at(k):
+        d = scenes.hole_desc(0.9, time=0.2 * k)
+        d.bloom = 4.5
+        return d
+
+    times, lens = [], []
+    try:
+        for k in range(warm + frames):
+            d = desc_at(k)
+            lib.artfCudaSceneSetBlackHole(scene, C.byref(d))
+            t0 = time.perf_counter()
+            if not vt.draw(r, scene) or not vt.readPixels(r, bgra.ctypes.data):
+                raise RuntimeError(lib.artfCudaLastError())
+            if k >= warm:
+                times.append((time.perf_counter() - t0) * 1e3)
+                st = capi.FrameStats()
+                vt.stats(r, C.cast(C.pointer(st), C.c_void_p))
+                lens.append(st.lensMs)
+    finally:
+        vt.destroy(r)
+        lib.artfCudaSceneFree(scene)
+    # the oracle port of the frame's parts on the host: a gas step, the trace (all host threads), bloom and
+    # tone map (one thread), on the synthetic disc of the same hole
+    view = scenes.Scene("frame", desc_at(warm), cam, w, h, seed=0)
+    frame, _, clamped = scenes.frame(view)
+    m = binding.synth_map(clamped.discInner, clamped.discOuter, clamped.spin, 0, 3.0)
+    fl = binding.Fluid(binding.oracle(), "oracle", clamped.discInner, clamped.discOuter, clamped.spin, 0.0)
+    t0 = time.perf_counter()
+    fl.advance(0.2 + 1e-3)
+    field, _ = fl.read()
+    t1 = time.perf_counter()
+    hdr = binding.render32(frame, m, field)
+    t2 = time.perf_counter()
+    binding.post(frame, hdr)
+    t3 = time.perf_counter()
+    fl.free()
+    return {"workload": "the reference's blackhole frame: 1920x1080, 1 ray a pixel, a = 0.9, i = 80 deg, r = 30 M, "
+                        "painted disc, a gas step a frame, bloom 4.5, ACES and dither to BGRA, read back to the host",
+            "ms_per_frame": statistics.median(times), "ms_per_frame_min": min(times), "lens_ms": statistics.median(lens),
+            "frames": frames,
+            "reference_published_ms": {"vega8_vulkan": 23.0, "ryzen_3200g_4_cores_software": 141.0},
+            "cpu_baseline": {"ms_per_frame": (t3 - t0) * 1e3, "fluid_step_ms": (t1 - t0) * 1e3,
+                             "trace_ms": (t2 - t1) * 1e3, "post_ms": (t3 - t2) * 1e3, "cores": os.cpu_count(),
+                             "kind": "port", "sample": "one frame: the oracle's gas step and bloom on one thread, "
+                                                       "its trace on all host threads"}}
 
 
 def fit_measurement(lib, ctx, fd_fits):
