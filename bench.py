@@ -58,9 +58,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--quick", action="store_true", help="skip the slow side measurements")
-    p.add_argument("--profile", choices=["mixed", "fp64", "exact", "fp32", "adjoint"],
+    p.add_argument("--profile", choices=["mixed", "fp64", "exact", "fp32", "adjoint", "frame"],
                    help="trace one frame of that precision (after one untimed one), or run the adjoint twice, "
-                        "and exit: the case for ncu")
+                        "or draw five of the reference's frames through the backend, and exit: the case for ncu")
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--views", type=int, default=1, help="views of --profile adjoint")
@@ -302,6 +302,11 @@ def profile_case(args):
     lib = capi.load()
     ctx = C.c_void_p()
     capi.check(lib.artfCudaCreate(0, C.byref(ctx)))
+    if args.profile == "frame":
+        out = reference_frame_measurement(lib, frames=3, warm=2, cpu=False)
+        print(json.dumps({"profile": "frame", **{k: v for k, v in out.items() if k.endswith("ms")}}))
+        lib.artfCudaDestroy(ctx)
+        return
     if args.profile == "adjoint":
         from artful_gb300 import fit
         target, start = fit.config4_params()
@@ -848,7 +853,7 @@ def next_rows_measurement(lib, ctx):
                              "kind": "port", "sample": "one painted map; 48 fluid steps"}}
 
 
-def reference_frame_measurement(lib, frames=30, warm=5):
+def reference_frame_measurement(lib, frames=30, warm=5, cpu=True):
     """The reference's own published frame (its README's `blackhole` figure: 1920 x 1080, one ray a pixel,
     a fluid step and bloom; 23 ms on a Vega 8 in Vulkan, 141 ms in its software renderer on a 4-core Ryzen
     3200G), drawn through this backend's eight-entry table with device inputs: the reference's own scene (its
@@ -856,7 +861,6 @@ def reference_frame_measurement(lib, frames=30, warm=5):
     tone map and dither, the BGRA frame read back to the host every frame.  The hole's clock moves one gas
     step (0.2) a frame.  Beside it the oracle port of the same frame's parts on the host cores."""
     from artful_gb300 import capi, scenes
-    from oracle import binding
     w, h = 1920, 1080
     opts = capi.RendererOptions(4)
     opts.width, opts.height = w, h
@@ -875,24 +879,46 @@ def reference_frame_measurement(lib, frames=30, warm=5):
         d.bloom = 4.5
         return d
 
-    times, lens = [], []
+    import torch
+    pinned = torch.empty((h, w), dtype=torch.int32, pin_memory=True)
+    times, draws, reads, lens, pinned_times = [], [], [], [], []
     try:
-        for k in range(warm + frames):
+        for k in range(warm + 2 * frames):
             d = desc_at(k)
             lib.artfCudaSceneSetBlackHole(scene, C.byref(d))
+            # the first frames read back into pageable memory (a plain host array), the rest into pinned
+            into = bgra.ctypes.data if k < warm + frames else pinned.data_ptr()
             t0 = time.perf_counter()
-            if not vt.draw(r, scene) or not vt.readPixels(r, bgra.ctypes.data):
+            if not vt.draw(r, scene):
                 raise RuntimeError(lib.artfCudaLastError())
-            if k >= warm:
-                times.append((time.perf_counter() - t0) * 1e3)
+            t1 = time.perf_counter()
+            if not vt.readPixels(r, into):
+                raise RuntimeError(lib.artfCudaLastError())
+            t2 = time.perf_counter()
+            if warm <= k < warm + frames:
+                times.append((t2 - t0) * 1e3)
+                draws.append((t1 - t0) * 1e3)
+                reads.append((t2 - t1) * 1e3)
                 st = capi.FrameStats()
                 vt.stats(r, C.cast(C.pointer(st), C.c_void_p))
                 lens.append(st.lensMs)
+            elif k >= warm + frames:
+                pinned_times.append((t2 - t0) * 1e3)
     finally:
         vt.destroy(r)
         lib.artfCudaSceneFree(scene)
+    out = {"workload": "the reference's blackhole frame: 1920x1080, 1 ray a pixel, a = 0.9, i = 80 deg, r = 30 M, "
+                       "painted disc, a gas step a frame, bloom 4.5, ACES and dither to BGRA, read back to the host",
+           "ms_per_frame": statistics.median(times), "ms_per_frame_min": min(times),
+           "draw_ms": statistics.median(draws), "read_pixels_ms": statistics.median(reads),
+           "lens_ms": statistics.median(lens), "frames": frames,
+           "ms_per_frame_into_pinned": statistics.median(pinned_times),
+           "reference_published_ms": {"vega8_vulkan": 23.0, "ryzen_3200g_4_cores_software": 141.0}}
+    if not cpu:
+        return out
     # the oracle port of the frame's parts on the host: a gas step, the trace (all host threads), bloom and
     # tone map (one thread), on the synthetic disc of the same hole
+    from oracle import binding
     view = scenes.Scene("frame", desc_at(warm), cam, w, h, seed=0)
     frame, _, clamped = scenes.frame(view)
     m = binding.synth_map(clamped.discInner, clamped.discOuter, clamped.spin, 0, 3.0)
@@ -906,15 +932,11 @@ def reference_frame_measurement(lib, frames=30, warm=5):
     binding.post(frame, hdr)
     t3 = time.perf_counter()
     fl.free()
-    return {"workload": "the reference's blackhole frame: 1920x1080, 1 ray a pixel, a = 0.9, i = 80 deg, r = 30 M, "
-                        "painted disc, a gas step a frame, bloom 4.5, ACES and dither to BGRA, read back to the host",
-            "ms_per_frame": statistics.median(times), "ms_per_frame_min": min(times), "lens_ms": statistics.median(lens),
-            "frames": frames,
-            "reference_published_ms": {"vega8_vulkan": 23.0, "ryzen_3200g_4_cores_software": 141.0},
-            "cpu_baseline": {"ms_per_frame": (t3 - t0) * 1e3, "fluid_step_ms": (t1 - t0) * 1e3,
+    out["cpu_baseline"] = {"ms_per_frame": (t3 - t0) * 1e3, "fluid_step_ms": (t1 - t0) * 1e3,
                              "trace_ms": (t2 - t1) * 1e3, "post_ms": (t3 - t2) * 1e3, "cores": os.cpu_count(),
                              "kind": "port", "sample": "one frame: the oracle's gas step and bloom on one thread, "
-                                                       "its trace on all host threads"}}
+                                                       "its trace on all host threads"}
+    return out
 
 
 def fit_measurement(lib, ctx, fd_fits):
