@@ -44,9 +44,9 @@ WORKLOAD = "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50 M, i=85 d
 # Kernels one mixed frame launches: the tile probe, the heavy-first order, the trace, the ray-plane sum.
 LAUNCHES_PER_MIXED_FRAME = 4
 # DRAM bytes (read + write) of one launch of the mixed trace kernel at this workload, from one ncu
-# capture (dram__bytes_read.sum 17.85 MB + dram__bytes_write.sum 73.76 MB): the map read once, and the
+# capture (dram__bytes_read.sum 17.71 MB + dram__bytes_write.sum 74.34 MB): the map read once, and the
 # part of the 133 MB of ray planes that leaves L2 before the sum reads it back.
-TRACE_TRAFFIC_BYTES = 91_610_000
+TRACE_TRAFFIC_BYTES = 92_050_000
 TRACE_TRAFFIC_GEODESICS = 1920 * 1080 * 4
 TRACE_TRAFFIC_SOURCE = "ncu dram__bytes of one launch of the mixed trace kernel at 1920x1080 x 4 jittered rays"
 
