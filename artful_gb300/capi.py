@@ -75,6 +75,7 @@ class TraceOptions(C.Structure):
 
 
 ORDER_HEAVY_FIRST, ORDER_PIXELS = 0, 1
+BACKEND = 4  # ARTF_CUDA_BACKEND: Artful's ArtfBackend with this backend appended (artful_cuda_renderer.h)
 GUARD_MOTION, GUARD_HORIZON, GUARD_RADIAL, GUARD_POLAR, GUARD_PSI, GUARD_ALL = 1, 2, 4, 8, 16, 31
 
 

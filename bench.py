@@ -862,7 +862,7 @@ def reference_frame_measurement(lib, frames=30, warm=5, cpu=True):
     step (0.2) a frame.  Beside it the oracle port of the same frame's parts on the host cores."""
     from artful_gb300 import capi, scenes
     w, h = 1920, 1080
-    opts = capi.RendererOptions(4)
+    opts = capi.RendererOptions(capi.BACKEND)
     opts.width, opts.height = w, h
     r = lib.artfCudaNew(C.byref(opts))
     if not r:

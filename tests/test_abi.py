@@ -58,3 +58,21 @@ def test_create_reports_no_device_here(lib):
     h = C.c_void_p()
     assert lib.artfCudaCreate(0, C.byref(h)) == -2
     assert not h.value
+
+
+def test_enumerations_match_the_headers():
+    """The Python constants the harness passes are the values the headers give."""
+    text = ""
+    for header in ("artful_cuda.h", "artful_cuda_renderer.h"):
+        text += open(os.path.join(ROOT, "include", header)).read()
+
+    def value(name):
+        m = re.search(r"\b" + name + r"\s*=\s*(\d+)", text)
+        assert m, name
+        return int(m.group(1))
+
+    assert capi.BACKEND == value("ARTF_CUDA_BACKEND")
+    assert (capi.EXACT, capi.FP32, capi.FP64, capi.MIXED) == tuple(
+        value(n) for n in ("ARTF_CUDA_EXACT", "ARTF_CUDA_FP32", "ARTF_CUDA_FP64", "ARTF_CUDA_MIXED"))
+    assert (capi.ORDER_HEAVY_FIRST, capi.ORDER_PIXELS) == (value("ARTF_CUDA_ORDER_HEAVY_FIRST"),
+                                                           value("ARTF_CUDA_ORDER_PIXELS"))

@@ -20,7 +20,7 @@ class Backend:
 
     def __init__(self, lib, width, height):
         self.lib = lib
-        opts = capi.RendererOptions(capi.ARTF_CUDA_BACKEND if hasattr(capi, "ARTF_CUDA_BACKEND") else 4)
+        opts = capi.RendererOptions(capi.BACKEND)
         opts.width, opts.height = width, height
         self.ptr = lib.artfCudaNew(C.byref(opts))
         assert self.ptr, lib.artfCudaLastError()
