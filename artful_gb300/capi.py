@@ -183,6 +183,7 @@ SIGNATURES = {
     "artfCudaUseFluid": (C.c_int, [_vp, _vp]),
     # the renderer backend (artful_cuda_renderer.h)
     "artfCudaRendererSetDeviceInputs": (None, [_vp, C.c_bool]),
+    "artfCudaFrameRead": (C.c_int, [_vp, _vp, _vp]),
     "artfCudaNew": (_vp, [_vp]),
     "artfCudaNewWithReader": (_vp, [_vp, _vp]),
     "artfCudaRendererReadLight": (C.c_bool, [_vp, _vp]),

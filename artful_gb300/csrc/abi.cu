@@ -46,6 +46,8 @@ struct ArtfCuda {
     size_t hdrPixels;
     uint32_t* bgra;               /* the draw path's tone-mapped frame */
     size_t bgraPixels;
+    size_t drawnPixels;           /* the last artfCudaHoleDraw's frame size (its light in hdr, its BGRA in
+                                   * bgra), for artfCudaFrameRead; 0: none since */
     float* bloom;                 /* three planes of bloomPixels floats */
     size_t bloomPixels;
     /* the mixed trace's view table: device copy, pinned staging, and when the staging was last read */
@@ -554,6 +556,7 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
     if (!hostHdr) return fail(ARTF_CUDA_EINVAL, "hostHdr is NULL");
+    ctx->drawnPixels = 0; /* (the light buffer is this path's from here on) */
     if ((status = hostInputs(ctx, hostMap, mapVersion, hostFluid, fluidVersion))) return status;
     const size_t pixels = (size_t)frame->size[0] * frame->size[1];
     if (pixels > ctx->hdrPixels) {
@@ -590,6 +593,7 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
     int status = enter(ctx);
     if (status) return status;
     if ((status = checkFrame(frame, options))) return status;
+    ctx->drawnPixels = 0;
     if ((status = hostInputs(ctx, hostMap, mapVersion, hostFluid, fluidVersion))) return status;
     const size_t pixels = (size_t)frame->size[0] * frame->size[1];
     size_t bloomPixels = 0;
@@ -620,6 +624,22 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
                                                    cudaMemcpyDeviceToHost, ctx->stream));
     if (hostBgra)
         CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostBgra, ctx->bgra, sizeof(uint32_t) * pixels,
+                                                   cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+    ctx->drawnPixels = pixels;
+    return ARTF_CUDA_OK;
+}
+
+extern "C" int artfCudaFrameRead(ArtfCuda* ctx, float* hostHdr, uint32_t* hostBgra) {
+    artf::Range range("artfCudaFrameRead");
+    int status = enter(ctx);
+    if (status) return status;
+    if (!ctx->drawnPixels) return fail(ARTF_CUDA_EINVAL, "no frame drawn since the frame buffers last changed");
+    if (hostHdr)
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostHdr, ctx->hdr, sizeof(float4) * ctx->drawnPixels,
+                                                   cudaMemcpyDeviceToHost, ctx->stream));
+    if (hostBgra)
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaMemcpyAsync(hostBgra, ctx->bgra, sizeof(uint32_t) * ctx->drawnPixels,
                                                    cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
     return ARTF_CUDA_OK;

@@ -153,6 +153,8 @@ typedef struct CudaRenderer {
     int precision;
     uint32_t* bgra;
     float* light;
+    bool bgraOnDevice;          /* the last frame's BGRA is the context's (read back at readPixels), not bgra */
+    bool lightOnDevice;         /* the last frame's light is the context's, not light */
     uint32_t* overlay;          /* a copy of the last overlay, width * height, or NULL */
     int overlayWidth, overlayHeight;
     char description[160];
@@ -186,6 +188,7 @@ static bool allocFrame(CudaRenderer* c, int width, int height) {
     free(c->light);
     c->bgra = bgra;
     c->light = light;
+    c->bgraOnDevice = c->lightOnDevice = false;
     c->width = width > 0 ? width : 1;
     c->height = height > 0 ? height : 1;
     return true;
@@ -287,6 +290,7 @@ static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
     ArtfCudaHoleInputs in;
     memset(&c->stats, 0, sizeof c->stats);
     if (!c->reader(scene, &in) || !in.on) {
+        c->bgraOnDevice = c->lightOnDevice = false;
         for (size_t i = 0; i < (size_t)c->width * c->height; ++i) c->bgra[i] = 0xFF000000u;
         memset(c->light, 0, sizeof(float) * 4 * (size_t)c->width * c->height);
         composite(c);
@@ -310,12 +314,18 @@ static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
     options.stepScale = 1.f;
     options.persistent = 1;
     ArtfCudaTraceStats stats;
+    /* The frame stays on the device until readPixels (or the light until artfCudaRendererReadLight) asks
+     * for it; with an overlay the BGRA comes back now, to be composited as drawn. */
+    uint32_t* bgraNow = c->overlay ? c->bgra : NULL;
+    c->bgraOnDevice = c->lightOnDevice = false;
     const int status = c->deviceInputs
-                           ? artfCudaHoleDraw(c->ctx, &frame, &frame64, NULL, 0, NULL, 0, &options, c->light, c->bgra,
+                           ? artfCudaHoleDraw(c->ctx, &frame, &frame64, NULL, 0, NULL, 0, &options, NULL, bgraNow,
                                               &stats)
                            : artfCudaHoleDraw(c->ctx, &frame, &frame64, in.map, in.mapVersion, in.fluid,
-                                              in.fluidVersion, &options, c->light, c->bgra, &stats);
+                                              in.fluidVersion, &options, NULL, bgraNow, &stats);
     if (status) return false; /* the device is lost (or unusable): the renderer must be freed */
+    c->bgraOnDevice = bgraNow == NULL;
+    c->lightOnDevice = true;
     composite(c);
     c->stats.lensMs = stats.ms;
     c->stats.gpuMs = stats.ms;
@@ -327,6 +337,7 @@ static bool cudaDraw(ArtfCudaRenderer* r, void* scene) {
 static bool cudaReadPixels(ArtfCudaRenderer* r, uint32_t* dst) {
     CudaRenderer* c = (CudaRenderer*)r;
     if (!dst) return false;
+    if (c->bgraOnDevice) return artfCudaFrameRead(c->ctx, NULL, dst) == ARTF_CUDA_OK;
     memcpy(dst, c->bgra, sizeof(uint32_t) * (size_t)c->width * c->height);
     return true;
 }
@@ -379,6 +390,7 @@ ArtfCudaRenderer* artfCudaNew(const ArtfCudaRendererOptions* options) {
 bool artfCudaRendererReadLight(ArtfCudaRenderer* r, float* dst) {
     CudaRenderer* c = (CudaRenderer*)r;
     if (!c || !dst) return false;
+    if (c->lightOnDevice) return artfCudaFrameRead(c->ctx, dst, NULL) == ARTF_CUDA_OK;
     memcpy(dst, c->light, sizeof(float) * 4 * (size_t)c->width * c->height);
     return true;
 }

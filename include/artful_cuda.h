@@ -280,6 +280,13 @@ int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCu
                      const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                      const ArtfCudaTraceOptions* options, float* hostHdr, uint32_t* hostBgra,
                      ArtfCudaTraceStats* stats);
+/* The last frame artfCudaHoleDraw drew on this context, copied back when it is wanted rather than at
+ * every draw: its linear light (width * height float4) to hostHdr and its BGRA (width * height uint32)
+ * to hostBgra, each when not NULL.  ARTF_CUDA_EINVAL when no draw has finished since the context's frame
+ * buffers last changed (artfCudaHoleRender uses the light buffer too).  Synchronous.  (The renderer's
+ * readPixels, software.c's frame in host memory, has no counterpart call in the reference: a GPU
+ * backend's frame is read back at readPixels.) */
+int artfCudaFrameRead(ArtfCuda* ctx, float* hostHdr, uint32_t* hostBgra);
 /* The bloom and tone map alone, on device buffers: hdr (width * height float4) to bgra, with three bloom
  * planes of the frame's bloom pixel count (artfCudaHoleFrame's return value), on `stream`. */
 int artfCudaPostLaunch(const ArtfCudaHoleFrame* frame, const float* hdr, float* const bloomPlanes[3], uint32_t* bgra,

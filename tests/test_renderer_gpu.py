@@ -236,3 +236,32 @@ def test_draw_with_what_the_context_holds(lib, ctx, golden):
     capi.check(lib.artfCudaHoleDraw(ctx, C.byref(frame), C.byref(frame64), None, 0, None, 0, C.byref(opts), None,
                                     bgra.ctypes.data, None))
     assert hashlib.sha256(bgra.tobytes()).hexdigest() == meta["draw"]["c1_bloom"]["bgra_sha256"]
+
+
+def test_frame_read_after_a_draw(lib, ctx, golden):
+    """A draw that copies nothing back leaves its frame on the device; artfCudaFrameRead returns the same
+    light and BGRA a draw into host buffers gives, and refuses once the light buffer has been reused."""
+    meta, _ = golden
+    view = _draw_case("c1_bloom")
+    frame, frame64, clamped = scenes.frame(view)
+    m = scenes.synth_map(lib, clamped, view.seed, view.emissivity)
+    fluid = scenes.unit_fluid()
+    opts = capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 1)
+    shape = (view.height, view.width)
+    light, bgra = np.zeros(shape + (4,), np.float32), np.zeros(shape, np.uint32)
+    capi.check(lib.artfCudaHoleDraw(ctx, C.byref(frame), C.byref(frame64), m.ctypes.data, 0, fluid.ctypes.data, 0,
+                                    C.byref(opts), light.ctypes.data, bgra.ctypes.data, None))
+    capi.check(lib.artfCudaHoleDraw(ctx, C.byref(frame), C.byref(frame64), m.ctypes.data, 0, fluid.ctypes.data, 0,
+                                    C.byref(opts), None, None, None))
+    light2, bgra2 = np.zeros_like(light), np.zeros_like(bgra)
+    capi.check(lib.artfCudaFrameRead(ctx, light2.ctypes.data, bgra2.ctypes.data))
+    assert np.array_equal(bgra2, bgra) and np.array_equal(light2.view(np.uint32), light.view(np.uint32))
+    assert hashlib.sha256(bgra2.tobytes()).hexdigest() == meta["draw"]["c1_bloom"]["bgra_sha256"]
+    only = np.zeros_like(bgra)
+    capi.check(lib.artfCudaFrameRead(ctx, None, only.ctypes.data))
+    assert np.array_equal(only, bgra)
+    # the host path's render reuses the light buffer: nothing drawn to read any more
+    capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), C.byref(frame64), m.ctypes.data, 0, fluid.ctypes.data, 0,
+                                      C.byref(opts), light2.ctypes.data, None))
+    assert lib.artfCudaFrameRead(ctx, None, only.ctypes.data) == -1
+    assert b"no frame drawn" in lib.artfCudaLastError()
