@@ -121,15 +121,29 @@ __global__ void __launch_bounds__(256) seedDensity(float* __restrict__ s, const 
     s[cell] = .06f + 3.4f * ease(.34f, .68f, v) * ease(.34f, .68f, v);
 }
 
-/* fluid.c:202-218: eddies one after another (they overlap), each one's cells at once; one block. */
+/* fluid.c:202-218: eddies one after another (they overlap), each one's cells at once; one block.  The
+ * rows an eddy can reach (its radial test passed) are found first and only they are visited: the test
+ * still runs on each, so every cell gets the update the reference gives it. */
 __global__ void __launch_bounds__(1024) stir(float* __restrict__ s, float* __restrict__ vr, float* __restrict__ w,
                                              const Rings* __restrict__ rings, const Eddy* __restrict__ eddies,
                                              int count) {
+    __shared__ int lo, hi;
     for (int e = 0; e < count; ++e) {
         const Eddy q = eddies[e];
+        if (threadIdx.x == 0) lo = FH, hi = -1;
+        __syncthreads();
+        if ((int)threadIdx.x < FH) {
+            const float dr = rings->radius[threadIdx.x] - q.r0;
+            if (!(dr * dr > 6.25f * q.size * q.size)) {
+                atomicMin(&lo, (int)threadIdx.x);
+                atomicMax(&hi, (int)threadIdx.x);
+            }
+        }
+        __syncthreads();
         const int span = 2 * q.reach + 1; /* columns -reach .. reach: fewer than FW, so each cell once */
-        for (int k = (int)threadIdx.x; k < FH * span; k += (int)blockDim.x) {
-            const int j = k / span, di = k - j * span - q.reach;
+        const int rows = hi - lo + 1;     /* (none reached: not positive) */
+        for (int k = (int)threadIdx.x; k < rows * span; k += (int)blockDim.x) {
+            const int row = k / span, j = lo + row, di = k - row * span - q.reach;
             const float dr = rings->radius[j] - q.r0;
             if (dr * dr > 6.25f * q.size * q.size) continue;
             const float dx = (float)di * rings->radius[j] * ARC;
