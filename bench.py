@@ -48,6 +48,12 @@ LAUNCHES_PER_MIXED_FRAME = 4
 # part of the 133 MB of ray planes that leaves L2 before the sum reads it back.
 TRACE_TRAFFIC_BYTES = 92_050_000
 TRACE_TRAFFIC_GEODESICS = 1920 * 1080 * 4
+# How busy the mixed trace keeps its pipes, from one ncu --set full capture of its kernel at 960x540 x 4
+# (the counted work's fraction above counts an FP64 estimate and its Newton step as one operation): the
+# FP64 pipe's instructions, the FP32 FMA pipe's cycles and the schedulers' issue slots, of peak.
+MIXED_PIPES_BUSY = {"fp64": 0.511, "fp32_fma": 0.317, "issue": 0.660,
+                    "source": "ncu sm__inst_executed_pipe_fp64, sm__pipe_fma_cycles_active, smsp__issue_active "
+                              "of traceMixedQueueOneAll at 960x540 x 4"}
 TRACE_TRAFFIC_SOURCE = "ncu dram__bytes of one launch of the mixed trace kernel at 1920x1080 x 4 jittered rays"
 
 
@@ -712,7 +718,8 @@ def main():
                      "fp32": {"achieved": achieved, "peak": peak, "frac": achieved / peak,
                               "flops_per_frame": s_mixed.flops},
                      "hbm": hbm,
-                     "time": "the whole timed step (probe, order, trace, combine)"},
+                     "time": "the whole timed step (probe, order, trace, combine)",
+                     "pipes_busy": MIXED_PIPES_BUSY},
         "e2e": {"value": world * geodesics / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": (map_.nbytes + fluid.nbytes), "d2h_bytes_per_step": h * w * 16},
         "gpu_launches": args.steps * LAUNCHES_PER_MIXED_FRAME,
