@@ -559,6 +559,18 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
     ctx->drawnPixels = 0; /* (the light buffer is this path's from here on) */
     if ((status = hostInputs(ctx, hostMap, mapVersion, hostFluid, fluidVersion))) return status;
     const size_t pixels = (size_t)frame->size[0] * frame->size[1];
+    /* A page-locked host buffer, which the device addresses, takes the frame straight from the trace's
+     * kernels, over the link as they write it; any other buffer gets a copy of the device's frame. */
+    cudaPointerAttributes where;
+    if (cudaPointerGetAttributes(&where, hostHdr) == cudaSuccess && where.type == cudaMemoryTypeHost &&
+        where.devicePointer) {
+        if ((status = artfCudaHoleTrace(ctx, frame, frame64, nullptr, nullptr, options, (float*)where.devicePointer,
+                                        nullptr, stats)))
+            return status;
+        CUDA_OR(ARTF_CUDA_ELAUNCH, cudaStreamSynchronize(ctx->stream));
+        return ARTF_CUDA_OK;
+    }
+    cudaGetLastError(); /* (a pointer the runtime does not know is no error to keep) */
     if (pixels > ctx->hdrPixels) {
         cudaFree(ctx->hdr);
         ctx->hdr = nullptr;

@@ -356,7 +356,9 @@ int artfCudaAutotune(ArtfCuda* ctx, const ArtfCudaView* views, int count, const 
                      ArtfCudaTuning* result);
 
 /* The same from host memory to host memory: copies the map and fluid (when their versions changed; NULL:
- * the context's own), traces, and copies width * height float4 back to `hostHdr`.  Synchronous. */
+ * the context's own), traces, and brings width * height float4 back to `hostHdr`: a page-locked buffer
+ * (cudaHostAlloc, or registered) is written by the trace's kernels directly, any other is copied into
+ * from the device's frame.  Synchronous. */
 int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, const ArtfCudaHoleFrame64* frame64,
                        const float* hostMap, uint64_t mapVersion, const float* hostFluid, uint64_t fluidVersion,
                        const ArtfCudaTraceOptions* options, float* hostHdr, ArtfCudaTraceStats* stats);

@@ -183,6 +183,23 @@ def test_host_path_equals_device_path(lib, ctx):
     assert np.array_equal(out.view(np.uint32), hdr.view(np.uint32))
 
 
+def test_host_path_into_page_locked_memory(lib, ctx):
+    """Into a page-locked buffer the trace's kernels write the frame directly: the same bits as the copy
+    into a plain array, for the exact trace and for the mixed one with its ray planes."""
+    import ctypes as C
+    import torch
+    scene, frame, frame64, m, fluid = _scene_inputs(lib, "c1")
+    for opts in (capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 1),
+                 capi.TraceOptions(capi.MIXED, 4, 5, 1.0, 0.0, 0, 0, 1)):
+        plain = np.zeros((scene.height, scene.width, 4), np.float32)
+        locked = torch.zeros((scene.height, scene.width, 4), dtype=torch.float32).pin_memory()
+        for buf in (plain.ctypes.data, locked.data_ptr()):
+            capi.check(lib.artfCudaHoleRender(ctx, C.byref(frame), None, m.ctypes.data, 0, fluid.ctypes.data, 0,
+                                              C.byref(opts), buf, None))
+        assert np.array_equal(plain.view(np.uint32), locked.numpy().view(np.uint32))
+        assert plain[..., :3].sum() > 0
+
+
 def test_bad_options_are_refused(lib, ctx):
     import ctypes as C
     scene, frame, frame64, m, fluid = _scene_inputs(lib, "odd_3x2")
