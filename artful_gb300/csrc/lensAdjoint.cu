@@ -8,9 +8,11 @@
  * the host supplies), through the rings' glow (r / inner)^-q and orbit speed, evaluated here from their
  * formulas, and through the spin in the equations of motion.
  *
- * Each thread traces its pixel's ray forward, keeping the ray's state at every step of the current
- * segment of K steps and a checkpoint at each segment's start; then walks back: the last segment from
- * what it kept, each earlier one recomputed from its checkpoint.  At each step, in reverse order, it
+ * Two kernels.  The forward one traces each pixel's ray with its shading, keeps a checkpoint at the start
+ * of each segment of K steps in a trail in device memory (field by field across rays), and leaves the
+ * ray's loss adjoint and end there.  The reverse one walks each ray back from its last step that added
+ * radiance, a segment at a time, each segment recomputed from its checkpoint into a ring of K kept
+ * states in the thread's local memory.  At each step, in reverse order, it
  * applies the transposed derivatives of the sky (at the escape), of the disc crossing (its three slices,
  * the ring's glow and the Doppler shift) and of the Nystrom step's radial and polar parts, accumulating
  * the adjoints of the constants of motion; at the ray's start it takes them through the set-up to the
@@ -18,10 +20,10 @@
  * derivative (which texel or star cell, the 0.004 opacity cut-off, the step cap) contribute none: the
  * pathwise derivative.
  *
- * Work layout: a view table in device memory; grid (blocks of four 8 x 4 tiles, views), each block
- * copying its view's entry to shared memory, each warp tracing one tile.  Each tile's six sums go to the
- * tile's own slot; a second kernel adds them in a fixed order, in double, so the result does not depend
- * on scheduling. */
+ * Work layout: a view table in device memory; grid (blocks of four 8 x 4 tiles, views), the tiles of a
+ * view heaviest first, each block copying its view's entry to shared memory, each warp tracing one tile.
+ * Each tile's six sums go to the tile's own slot; a last kernel adds them in a fixed order, in double, so
+ * the result does not depend on scheduling. */
 #include "lensKernel.cuh"
 #include "lensTangent.h"
 
