@@ -46,6 +46,8 @@ def test_argument_errors_without_a_device(lib):
     assert lib.artfCudaSetMap(None, None, 0) == -1
     assert lib.artfCudaHoleTrace(None, None, None, None, None, None, None, None, None) == -1
     assert b"context" in lib.artfCudaLastError()
+    assert lib.artfCudaFrameRead(None, None, None) == -1
+    assert b"context" in lib.artfCudaLastError()
 
 
 def test_create_reports_no_device_here(lib):
