@@ -332,7 +332,9 @@ int artfCudaFluidClock(double* clock, double time) {
         if (time < *clock - 8.0) *clock = time;
         return 0;
     }
-    int steps = (int)((time - *clock) / FLUID_STEP);
+    /* (the gap in steps is capped before it becomes an int: a clock far ahead would overflow one) */
+    const double gap = (time - *clock) / FLUID_STEP;
+    int steps = gap >= (double)(FLUID_MOST_STEPS + 1) ? FLUID_MOST_STEPS + 1 : (int)gap;
     if (steps > FLUID_MOST_STEPS) {
         *clock = time - (double)FLUID_MOST_STEPS * FLUID_STEP;
         steps = FLUID_MOST_STEPS;
