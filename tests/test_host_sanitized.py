@@ -1,5 +1,6 @@
-"""The library's host C11 code (the frame set-up, clamps, parameter scenes and synthetic maps) run over
-ordinary and edge inputs under AddressSanitizer and UndefinedBehaviorSanitizer: no report, exit 0."""
+"""The library's host C11 code run under AddressSanitizer and UndefinedBehaviorSanitizer: the frame set-up,
+clamps, parameter scenes and synthetic maps over ordinary and edge inputs, and the renderer backend's host
+logic through its table over a fake device.  No report, exit 0."""
 import os
 import subprocess
 
@@ -9,12 +10,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "artful_gb300", "csrc")
 
 
-def test_host_code_under_sanitizers(tmp_path):
-    exe = str(tmp_path / "host_sanitized")
+def _build_and_run(tmp_path, driver, units):
+    exe = str(tmp_path / driver.replace(".c", ""))
     cmd = [os.environ.get("CC", "gcc"), "-std=c11", "-O1", "-g", "-fno-omit-frame-pointer",
            "-fsanitize=address,undefined,float-cast-overflow", "-fno-sanitize-recover=all", "-ffp-contract=off",
-           "-I" + os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "host_sanitized.c"),
-           os.path.join(CSRC, "holeHost.c"), os.path.join(CSRC, "synthScene.c"), "-lm", "-o", exe]
+           "-I" + os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", driver)] + \
+          [os.path.join(CSRC, u) for u in units] + ["-lm", "-o", exe]
     build = subprocess.run(cmd, capture_output=True, text=True)
     if build.returncode != 0 and "sanitize" in build.stderr:
         pytest.skip("this compiler has no sanitizer runtime")
@@ -23,4 +24,13 @@ def test_host_code_under_sanitizers(tmp_path):
                          env=dict(os.environ, ASAN_OPTIONS="detect_leaks=1", UBSAN_OPTIONS="print_stacktrace=1"))
     assert run.returncode == 0, run.stdout + run.stderr
     assert "runtime error" not in run.stderr and "AddressSanitizer" not in run.stderr, run.stderr
-    assert run.stdout.startswith("checksum ")
+    return run.stdout
+
+
+def test_host_code_under_sanitizers(tmp_path):
+    assert _build_and_run(tmp_path, "host_sanitized.c", ["holeHost.c", "synthScene.c"]).startswith("checksum ")
+
+
+def test_renderer_host_logic_under_sanitizers(tmp_path):
+    out = _build_and_run(tmp_path, "renderer_sanitized.c", ["renderer.c", "holeHost.c", "synthScene.c"])
+    assert "renderer checks failed: 0" in out
