@@ -184,6 +184,7 @@ SIGNATURES = {
     # the renderer backend (artful_cuda_renderer.h)
     "artfCudaRendererSetDeviceInputs": (None, [_vp, C.c_bool]),
     "artfCudaFrameRead": (C.c_int, [_vp, _vp, _vp]),
+    "artfCudaFailAllocAfter": (C.c_int, [_vp, C.c_int]),
     "artfCudaNew": (_vp, [_vp]),
     "artfCudaNewWithReader": (_vp, [_vp, _vp]),
     "artfCudaRendererReadLight": (C.c_bool, [_vp, _vp]),

@@ -79,6 +79,7 @@ struct ArtfCuda {
     size_t adjTrailBytes;
     uint32_t lastBands; /* launches of the last trace (1 but for a frame in bands) */
     int launchesLeft; /* host-side fault injection: launches before the context reports loss; -1 off */
+    int allocsLeft;   /* host-side fault injection: allocations before the next one fails; -1 off */
     bool lost;
 };
 
@@ -108,6 +109,20 @@ extern "C" int artfCudaFailAfter(ArtfCuda* ctx, int launches) {
     return ARTF_CUDA_OK;
 }
 
+extern "C" int artfCudaFailAllocAfter(ArtfCuda* ctx, int allocations) {
+    if (!ctx) return fail(ARTF_CUDA_EINVAL, "no context");
+    ctx->allocsLeft = allocations < 0 ? -1 : allocations;
+    return ARTF_CUDA_OK;
+}
+
+/* A context's device or page-locked allocation, counted against the injected-failure budget: when it has
+ * run out the allocation fails as an exhausted device's would, without the driver being asked. */
+static cudaError_t ctxAlloc(ArtfCuda* ctx, void** p, size_t bytes, bool pageLocked = false) {
+    if (ctx->allocsLeft == 0) return cudaErrorMemoryAllocation;
+    if (ctx->allocsLeft > 0) --ctx->allocsLeft;
+    return pageLocked ? cudaMallocHost(p, bytes) : cudaMalloc(p, bytes);
+}
+
 extern "C" int artfCudaCreate(int device, ArtfCuda** out) {
     if (!out) return fail(ARTF_CUDA_EINVAL, "out is NULL");
     *out = nullptr;
@@ -125,6 +140,7 @@ extern "C" int artfCudaCreate(int device, ArtfCuda** out) {
     ctx->device = device;
     ctx->smCount = prop.multiProcessorCount;
     ctx->launchesLeft = -1;
+    ctx->allocsLeft = -1;
     int status = ARTF_CUDA_OK;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->start) != cudaSuccess || cudaEventCreate(&ctx->stop) != cudaSuccess ||
@@ -286,8 +302,8 @@ static int reserveTable(ArtfCuda* ctx, int count) {
     cudaFreeHost(ctx->stage);
     ctx->table = ctx->stage = nullptr;
     ctx->tableBytes = 0;
-    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->table, bytes));
-    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->stage, bytes));
+    CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, &ctx->table, bytes));
+    CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, &ctx->stage, bytes, true));
     ctx->tableBytes = bytes;
     return ARTF_CUDA_OK;
 }
@@ -306,7 +322,7 @@ static int reservePlanes(ArtfCuda* ctx, size_t count) {
     cudaFree(ctx->planes); /* (synchronises: no launch still writes the old planes) */
     ctx->planes = nullptr;
     ctx->planeCount = 0;
-    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->planes, sizeof(float4) * count));
+    CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, (void**)&ctx->planes, sizeof(float4) * count));
     ctx->planeCount = count;
     return ARTF_CUDA_OK;
 }
@@ -318,7 +334,7 @@ static int reserveOrder(ArtfCuda* ctx, int tiles, int units) {
     cudaFree(ctx->order); /* (synchronises: no launch still reads the old order) */
     ctx->order = nullptr;
     ctx->orderBytes = 0;
-    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->order, bytes));
+    CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, &ctx->order, bytes));
     ctx->orderBytes = bytes;
     return ARTF_CUDA_OK;
 }
@@ -575,7 +591,7 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
         cudaFree(ctx->hdr);
         ctx->hdr = nullptr;
         ctx->hdrPixels = 0;
-        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->hdr, sizeof(float4) * pixels));
+        CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, (void**)&ctx->hdr, sizeof(float4) * pixels));
         ctx->hdrPixels = pixels;
     }
     if ((status = artfCudaHoleTrace(ctx, frame, frame64, nullptr, nullptr, options, (float*)ctx->hdr, nullptr, stats)))
@@ -587,12 +603,12 @@ extern "C" int artfCudaHoleRender(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame,
 }
 
 /* Grows a device buffer to at least `count` elements of `size` bytes. */
-static int reserve(void** buffer, size_t* held, size_t count, size_t size) {
+static int reserve(ArtfCuda* ctx, void** buffer, size_t* held, size_t count, size_t size) {
     if (count <= *held) return ARTF_CUDA_OK;
     cudaFree(*buffer);
     *buffer = nullptr;
     *held = 0;
-    CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(buffer, count * size));
+    CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, buffer, count * size));
     *held = count;
     return ARTF_CUDA_OK;
 }
@@ -612,9 +628,9 @@ extern "C" int artfCudaHoleDraw(ArtfCuda* ctx, const ArtfCudaHoleFrame* frame, c
     for (uint32_t i = 0; i < frame->size[3] && i < ARTF_CUDA_BLOOM_LEVELS; ++i)
         bloomPixels += (size_t)frame->bloom[i][1] * frame->bloom[i][2];
     if (frame->size[3] < 1 || bloomPixels == 0) return fail(ARTF_CUDA_EINVAL, "the frame has no bloom levels");
-    if ((status = reserve((void**)&ctx->hdr, &ctx->hdrPixels, pixels, sizeof(float4)))) return status;
-    if ((status = reserve((void**)&ctx->bgra, &ctx->bgraPixels, pixels, sizeof(uint32_t)))) return status;
-    if ((status = reserve((void**)&ctx->bloom, &ctx->bloomPixels, bloomPixels * 3, sizeof(float)))) return status;
+    if ((status = reserve(ctx, (void**)&ctx->hdr, &ctx->hdrPixels, pixels, sizeof(float4)))) return status;
+    if ((status = reserve(ctx, (void**)&ctx->bgra, &ctx->bgraPixels, pixels, sizeof(uint32_t)))) return status;
+    if ((status = reserve(ctx, (void**)&ctx->bloom, &ctx->bloomPixels, bloomPixels * 3, sizeof(float)))) return status;
     artf::TraceLaunch l = launchOf(ctx, options);
     l.frame = *frame;
     if (frame64) l.frame64 = *frame64;
@@ -690,8 +706,8 @@ static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int h
         cudaFreeHost(ctx->adjStage);
         ctx->adjTable = ctx->adjStage = nullptr;
         ctx->adjViews = 0;
-        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->adjTable, artf::adjointViewBytes() * count));
-        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->adjStage, artf::adjointViewBytes() * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, &ctx->adjTable, artf::adjointViewBytes() * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, &ctx->adjStage, artf::adjointViewBytes() * count, true));
         ctx->adjViews = (size_t)count;
     }
     if ((size_t)count > ctx->adjResultViews) {
@@ -699,15 +715,15 @@ static int reserveAdjoint(ArtfCuda* ctx, int count, int blocks, int width, int h
         cudaFreeHost(ctx->adjResultsHost);
         ctx->adjResults = ctx->adjResultsHost = nullptr;
         ctx->adjResultViews = 0;
-        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMalloc(&ctx->adjResults, sizeof(double) * 8 * count));
-        CUDA_OR(ARTF_CUDA_ENOMEM, cudaMallocHost(&ctx->adjResultsHost, sizeof(double) * 8 * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, (void**)&ctx->adjResults, sizeof(double) * 8 * count));
+        CUDA_OR(ARTF_CUDA_ENOMEM, ctxAlloc(ctx, (void**)&ctx->adjResultsHost, sizeof(double) * 8 * count, true));
         ctx->adjResultViews = (size_t)count;
     }
-    if (int s = reserve((void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float)))
+    if (int s = reserve(ctx, (void**)&ctx->adjPartials, &ctx->adjPartialCount, (size_t)count * blocks * 8, sizeof(float)))
         return s;
-    if (int s = reserve(&ctx->adjOrder, &ctx->adjOrderBytes, artf::adjointOrderBytes(count, width, height), 1))
+    if (int s = reserve(ctx, &ctx->adjOrder, &ctx->adjOrderBytes, artf::adjointOrderBytes(count, width, height), 1))
         return s;
-    return reserve(&ctx->adjTrail, &ctx->adjTrailBytes, artf::adjointTrailBytes(count, width, height, K), 1);
+    return reserve(ctx, &ctx->adjTrail, &ctx->adjTrailBytes, artf::adjointTrailBytes(count, width, height, K), 1);
 }
 
 extern "C" int artfCudaHoleAdjoint(ArtfCuda* ctx, const ArtfCudaHoleParams* params, int count, int width, int height,
@@ -890,8 +906,8 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
     const artf::TraceLaunch l = launchOf(ctx, options);
     const size_t planes = planesOf(l, views, count);
     g->planeCount = planes;
-    if (cudaMalloc(&g->table, bytes) != cudaSuccess || cudaMallocHost(&g->stage, bytes) != cudaSuccess ||
-        (planes && cudaMalloc(&g->planes, sizeof(float4) * planes) != cudaSuccess)) {
+    if (ctxAlloc(ctx, &g->table, bytes) != cudaSuccess || ctxAlloc(ctx, &g->stage, bytes, true) != cudaSuccess ||
+        (planes && ctxAlloc(ctx, (void**)&g->planes, sizeof(float4) * planes) != cudaSuccess)) {
         artfCudaBatchGraphDestroy(g);
         return fail(ARTF_CUDA_ENOMEM, "graph table allocation");
     }
@@ -899,7 +915,7 @@ extern "C" int artfCudaBatchGraphCreate(ArtfCuda* ctx, const ArtfCudaView* views
         artfCudaBatchGraphDestroy(g);
         return status;
     }
-    if (cudaMalloc(&g->order, artf::mixedOrderBytes(g->tiles, g->units)) != cudaSuccess) {
+    if (ctxAlloc(ctx, &g->order, artf::mixedOrderBytes(g->tiles, g->units)) != cudaSuccess) {
         artfCudaBatchGraphDestroy(g);
         return fail(ARTF_CUDA_ENOMEM, "graph order allocation");
     }

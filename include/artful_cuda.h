@@ -165,6 +165,11 @@ int artfCudaSetFluid(ArtfCuda* ctx, const float* hostFluid, uint64_t version);
  * src/render/rendererInternal.h:29-30): after `launches` more launches the context reports
  * ARTF_CUDA_ELOST, as after a device loss, without the GPU being touched.  -1 turns it off. */
 int artfCudaFailAfter(ArtfCuda* ctx, int launches);
+/* Allocation failure injected on the host (the reference counts allocations for its tests,
+ * src/core/base.c:32-33): after `allocations` more device or page-locked allocations the context's next
+ * one fails, as on an exhausted device, without the driver being asked, and the call reports
+ * ARTF_CUDA_ENOMEM; the context stays usable.  -1 turns it off. */
+int artfCudaFailAllocAfter(ArtfCuda* ctx, int allocations);
 /* The device copies, for callers that launch on their own buffers. */
 const float* artfCudaDeviceMap(const ArtfCuda* ctx);
 const float* artfCudaDeviceFluid(const ArtfCuda* ctx);

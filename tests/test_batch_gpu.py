@@ -143,6 +143,59 @@ def test_device_loss_injected_on_the_host(lib):
             lib.artfCudaDestroy(handle)
 
 
+def test_allocation_failure_injected_on_the_host(lib):
+    """With allocations made to fail on the host (artfCudaFailAllocAfter), each call that needs to grow a
+    buffer reports ARTF_CUDA_ENOMEM and nothing else: a failure at any point of the mixed trace's host
+    path (frame, view table, its staging, ray planes, order) or of the draw path leaves the context
+    usable, and once allowed again the same calls give the same bits as a context that never failed."""
+    scene = scenes.golden_scenes()["c1"]
+    frame, frame64, clamped = scenes.frame(scene)
+    m = scenes.synth_map(lib, clamped, scene.seed, scene.emissivity)
+    fluid = scenes.unit_fluid()
+    mixed = capi.TraceOptions(capi.MIXED, 4, 5, 1.0, 0.0, 0, 0, 1)
+    exact = capi.TraceOptions(capi.EXACT, 0, 0, 1.0, 0.0, 0, 0, 1)
+    shape = (scene.height, scene.width)
+
+    def render(handle):
+        hdr = np.zeros(shape + (4,), np.float32)
+        status = lib.artfCudaHoleRender(handle, C.byref(frame), None, m.ctypes.data, 0, fluid.ctypes.data, 0,
+                                        C.byref(mixed), hdr.ctypes.data, None)
+        return status, hdr
+
+    def draw(handle):
+        bgra = np.zeros(shape, np.uint32)
+        status = lib.artfCudaHoleDraw(handle, C.byref(frame), C.byref(frame64), m.ctypes.data, 0,
+                                      fluid.ctypes.data, 0, C.byref(exact), None, bgra.ctypes.data, None)
+        return status, bgra
+
+    clean = C.c_void_p()
+    capi.check(lib.artfCudaCreate(0, C.byref(clean)))
+    try:
+        want_hdr, want_bgra = render(clean)[1], draw(clean)[1]
+    finally:
+        lib.artfCudaDestroy(clean)
+    failures = 0
+    for budget in range(8):
+        handle = C.c_void_p()
+        capi.check(lib.artfCudaCreate(0, C.byref(handle)))
+        try:
+            capi.check(lib.artfCudaFailAllocAfter(handle, budget))
+            for call in (render, draw):
+                status, _ = call(handle)
+                assert status in (0, -3), status
+                failures += status == -3
+                if status == -3:
+                    assert b"memory" in lib.artfCudaLastError() or b"allocation" in lib.artfCudaLastError()
+            capi.check(lib.artfCudaFailAllocAfter(handle, -1))
+            status, hdr = render(handle)
+            assert status == 0 and np.array_equal(hdr.view(np.uint32), want_hdr.view(np.uint32))
+            status, bgra = draw(handle)
+            assert status == 0 and np.array_equal(bgra, want_bgra)
+        finally:
+            lib.artfCudaDestroy(handle)
+    assert failures >= 4  # (the early budgets fail the first call that allocates)
+
+
 @pytest.mark.parametrize("jitter", [0, 3])
 def test_heavy_first_gives_the_same_bits(lib, ctx, jitter):
     """The queue's order (ArtfCudaTraceOptions.order) changes when a ray is traced, never what it computes:
