@@ -190,7 +190,7 @@ __device__ __forceinline__ void accelBackWith(const BackTerms& t, float cc, cons
  * to those of (n, v) and the constants. */
 __device__ __forceinline__ void polarBack(const BackTerms& t, float big, const float* n, const float* v,
                                           const float* nNextBar, const float* vNextBar, const float* a1Extra,
-                                          float* nBar, float* vBar, ConstBar& g) {
+                                          bool extra, float* nBar, float* vBar, ConstBar& g, ConstBar& gs) {
     const float h = t.h, half = t.half, eighth = t.eighth, halfSq = t.halfSq, sixthSq = t.sixthSq, sixth = t.sixth;
     float a1[3], midN[3], a2s[3], endN[3], a3[3];
     const float c1 = accelWith(t, big, n, a1);
@@ -198,79 +198,73 @@ __device__ __forceinline__ void polarBack(const BackTerms& t, float big, const f
     const float c2 = accelWith(t, big, midN, a2s);
     for (int k = 0; k < 3; ++k) endN[k] = n[k] + h * v[k] + halfSq * a2s[k];
     const float c3 = accelWith(t, big, endN, a3);
-    float a1Bar[3], a2Bar[3], a3Bar[3], midBar[3] = {0.f, 0.f, 0.f}, endBar[3] = {0.f, 0.f, 0.f}, hBar = 0.f;
+    (void)a3;
+    float a1Bar[3], a2Bar[3], a3Bar[3], midBar[3] = {0.f, 0.f, 0.f}, endBar[3] = {0.f, 0.f, 0.f};
     for (int k = 0; k < 3; ++k) {
         /* n' = n + h v + h^2/6 (a1 + 2 a2);  v' = v + h/6 (a1 + a3 + 4 a2) */
         nBar[k] += nNextBar[k];
         vBar[k] += h * nNextBar[k] + vNextBar[k];
-        a1Bar[k] = sixthSq * nNextBar[k] + sixth * vNextBar[k] + a1Extra[k];
+        a1Bar[k] = sixthSq * nNextBar[k] + sixth * vNextBar[k];
         a2Bar[k] = 2.f * sixthSq * nNextBar[k] + 4.f * sixth * vNextBar[k];
         a3Bar[k] = sixth * vNextBar[k];
-        hBar += nNextBar[k] * (v[k] + h * (a1[k] + 2.f * a2s[k]) * (1.f / 3.f)) +
-                vNextBar[k] * (a1[k] + a3[k] + 4.f * a2s[k]) * (1.f / 6.f);
     }
-    accelBackWith(t, c3, endN, a3Bar, endBar, g);
+    accelBackWith(t, c3, endN, a3Bar, endBar, gs);
     for (int k = 0; k < 3; ++k) { /* endN = n + h v + h^2/2 a2 */
         nBar[k] += endBar[k];
         vBar[k] += h * endBar[k];
         a2Bar[k] += halfSq * endBar[k];
-        hBar += endBar[k] * (v[k] + h * a2s[k]);
     }
-    accelBackWith(t, c2, midN, a2Bar, midBar, g);
+    accelBackWith(t, c2, midN, a2Bar, midBar, gs);
     for (int k = 0; k < 3; ++k) { /* midN = n + h/2 v + h^2/8 a1 */
         nBar[k] += midBar[k];
         vBar[k] += half * midBar[k];
         a1Bar[k] += eighth * midBar[k];
-        hBar += midBar[k] * (.5f * v[k] + .25f * h * a1[k]);
     }
-    accelBackWith(t, c1, n, a1Bar, nBar, g);
-    g.step += hBar;
+    accelBackWith(t, c1, n, a1Bar, nBar, gs);
+    if (extra) accelBackWith(t, c1, n, a1Extra, nBar, g); /* (what a crossing read of a1: not the step's) */
 }
 
 /* The radial part: from the adjoints of (u', w', psi', drag') and of k1, adds to those of (u, w, psi,
  * drag) and the constants. */
 __device__ __forceinline__ void radialBack(const BackTerms& t, const RayConst<float>& c, float u, float w, float drag,
                                            float uNextBar, float wNextBar, float psiNextBar, float dragNextBar,
-                                           float k1Extra, float& uBar, float& wBar, float& psiBar, float& dragBar,
-                                           ConstBar& g) {
+                                           float k1Extra, bool extra, float& uBar, float& wBar, float& psiBar,
+                                           float& dragBar, ConstBar& g, ConstBar& gs) {
     const float h = t.h, half = t.half, eighth = t.eighth, halfSq = t.halfSq, sixthSq = t.sixthSq, sixth = t.sixth;
     const float k1 = bendAt(c, u);
     const float midU = u + half * w + eighth * k1;
     const float k2 = bendAt(c, midU);
     const float endU = u + h * w + halfSq * k2;
-    const float k3 = bendAt(c, endU);
-    float hBar = 0.f, midBar = 0.f;
+    float midBar = 0.f;
     if (t.a != 0.f) {
-        /* drag' = drag(u');  psi' = psi + h/6 (drag + drag' + 4 drag(midU)) */
+        /* drag' = drag(u');  psi' = psi + h/6 (drag + drag' + 4 drag(midU)): the step length's explicit
+         * share here; its share through u' and midU is the motion's, taken over the whole ray */
         const float uNext = u + h * w + sixthSq * (k1 + (k2 + k2));
         const DragTerms dNext = dragTerms(t.a, t.a2, c.xiA, uNext), dMid = dragTerms(t.a, t.a2, c.xiA, midU);
         const float s6 = psiNextBar * sixth;
         psiBar += psiNextBar;
         dragBar += s6;
-        hBar += psiNextBar * (drag + dNext.rate + 4.f * dMid.rate) * (1.f / 6.f);
+        g.step += psiNextBar * (drag + dNext.rate + 4.f * dMid.rate) * (1.f / 6.f);
         dragBackWith(t.a, c.xiA, midU, dMid, 4.f * s6, midBar, g);
         dragBackWith(t.a, c.xiA, uNext, dNext, dragNextBar + s6, uNextBar, g);
     }
     /* u' = u + h w + h^2/6 (k1 + 2 k2);  w' = w + h/6 (k1 + k3 + 4 k2) */
     uBar += uNextBar;
     wBar += h * uNextBar + wNextBar;
-    float k1Bar = sixthSq * uNextBar + sixth * wNextBar + k1Extra;
+    float k1Bar = sixthSq * uNextBar + sixth * wNextBar;
     float k2Bar = 2.f * sixthSq * uNextBar + 4.f * sixth * wNextBar;
     const float k3Bar = sixth * wNextBar;
-    hBar += uNextBar * (w + h * (k1 + 2.f * k2) * (1.f / 3.f)) + wNextBar * (k1 + k3 + 4.f * k2) * (1.f / 6.f);
     float endBar = 0.f; /* endU = u + h w + h^2/2 k2 */
-    bendBack(c, endU, k3Bar, endBar, g);
+    bendBack(c, endU, k3Bar, endBar, gs);
     uBar += endBar;
     wBar += h * endBar;
     k2Bar += halfSq * endBar;
-    hBar += endBar * (w + h * k2);
-    bendBack(c, midU, k2Bar, midBar, g); /* midU = u + h/2 w + h^2/8 k1 */
+    bendBack(c, midU, k2Bar, midBar, gs); /* midU = u + h/2 w + h^2/8 k1 */
     uBar += midBar;
     wBar += half * midBar;
     k1Bar += eighth * midBar;
-    hBar += midBar * (.5f * w + .25f * h * k1);
-    bendBack(c, u, k1Bar, uBar, g);
-    g.step += hBar;
+    bendBack(c, u, k1Bar, uBar, gs);
+    if (extra) bendBack(c, u, k1Extra, uBar, g); /* (what a crossing read of k1: not the step's) */
 }
 
 /* The adjoints of one step's start state and of what the crossing and the sky read of its end. */
@@ -907,9 +901,10 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
         Kept ring[kK ? kK : kMaxK];
         StepBar next;
         memset(&next, 0, sizeof next);
-        ConstBar g;
+        ConstBar g, gs; /* gs: what the steps' own maps give the constants the step length scales */
         memset(&g, 0, sizeof g);
-        float throughBar = 0.f;
+        memset(&gs, 0, sizeof gs);
+        float throughBar = 0.f, direct = 0.f; /* direct: velocities against what crossings add to their adjoints */
         for (int first = ((top - 1) / K) * K; first >= 0; first -= K) {
             const int last = min(first + K, top); /* steps first .. last - 1 */
             /* the segment's states from its kept start; the state after its last step is the ray's end
@@ -946,15 +941,28 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
                 if (escaped && step == steps - 1 && f.stars > 0.f)
                     skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
                 Crossing<float> x;
-                if (crossingOf(f, rhoScale, c, k.s, o, x))
+                const bool crossed = crossingOf(f, rhoScale, c, k.s, o, x);
+                if (crossed) {
                     crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
-                radialBack(bt, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, b.u, b.w,
-                           b.psi, b.drag, g);
-                polarBack(bt, c.big, k.s.n, k.s.v, b.nextN, next.v, b.a1, b.n, b.v, g);
+                    direct += k.s.w * b.w + k.s.v[0] * b.v[0] + k.s.v[1] * b.v[1] + k.s.v[2] * b.v[2];
+                }
+                radialBack(bt, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, crossed, b.u,
+                           b.w, b.psi, b.drag, g, gs);
+                polarBack(bt, c.big, k.s.n, k.s.v, b.nextN, next.v, b.a1, crossed, b.n, b.v, g, gs);
                 next = b;
                 after = k.s;
             }
         }
+        /* The step length's adjoint from the motion, over the whole ray at once.  A Nystrom step of length h
+         * is the step of length 1 of the motion with its velocities scaled by h and its accelerations'
+         * coefficients (K and a^2 for n; uA, uB, uC for u) by h^2, the velocities coming out divided by h;
+         * summed over the ray the terms telescope to the first state's velocities against their adjoints,
+         * less the velocities against what crossings added to their adjoints, and the scaled coefficients
+         * against what the steps gave their adjoints (for a: 2 a^2 d/d(a^2) = a d/da). */
+        g.step += (start.w * next.w + start.v[0] * next.v[0] + start.v[1] * next.v[1] + start.v[2] * next.v[2] -
+                   direct + 2.f * (c.uA * gs.uA + c.uB * gs.uB + c.uC * gs.uC + c.big * gs.big) + a * gs.a) /
+                  c.step;
+        g.a += gs.a, g.big += gs.big, g.uA += gs.uA, g.uB += gs.uB, g.uC += gs.uC;
         startBack(v, nx, ny, c, next, g, grad);
     }
     if (t.inside && v.pixelGrads)
