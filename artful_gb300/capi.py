@@ -113,7 +113,7 @@ class AdjointResult(C.Structure):
 
 
 GRAD_FIELDS = 28
-ADJOINT_MIN_CHECKPOINT, ADJOINT_MAX_CHECKPOINT, ADJOINT_MAX_VIEWS = 8, 64, 1024
+ADJOINT_MIN_CHECKPOINT, ADJOINT_MAX_CHECKPOINT, ADJOINT_MAX_VIEWS = 1, 64, 1024
 
 assert C.sizeof(HoleFrame) == 368 and C.sizeof(BlackHoleDesc) == 92 and C.sizeof(Camera) == 44
 assert C.sizeof(RayEnd) == 32 and C.sizeof(HoleParams) == 112 and C.sizeof(AdjointResult) == 48

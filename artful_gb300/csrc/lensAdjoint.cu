@@ -12,7 +12,9 @@
  * of each segment of K steps in a trail in device memory (field by field across rays), and leaves the
  * ray's loss adjoint and end there.  The reverse one walks each ray back from its last step that added
  * radiance, a segment at a time, each segment recomputed from its checkpoint into a ring of K kept
- * states in the thread's local memory.  At each step, in reverse order, it
+ * states in the thread's local memory; or, with K = 1 (every state kept, 48 bytes a step), a warp's rays
+ * together from the warp's highest step, their states read back through shared memory with nothing
+ * recomputed.  At each step, in reverse order, it
  * applies the transposed derivatives of the sky (at the escape), of the disc crossing (its three slices,
  * the ring's glow and the Doppler shift) and of the Nystrom step's radial and polar parts, accumulating
  * the adjoints of the constants of motion; at the ray's start it takes them through the set-up to the
@@ -48,6 +50,8 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kMaxK = ARTF_CUDA_ADJOINT_MAX_CHECKPOINT;
+/* With every state kept: the steps a warp's reads run ahead of its step back, through shared memory. */
+constexpr int kStage = 4;
 constexpr int kMaxSteps = 192;
 constexpr float kTurn = .15915494f; /* 1 / 2 pi, the reference's constant */
 
@@ -872,10 +876,12 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(con
     if ((threadIdx.x & 31) == 0) L.partials[t.tile * 8] = loss;
 }
 
-/* The reverse kernel: each ray's steps taken back from its last contributing one, a segment at a time,
- * each segment recomputed from its kept state into a ring of K states, then the ray's set-up; the tile's
- * gradient to its slot. */
-template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(const AdjointLaunch L) {
+/* The reverse kernel: each ray's steps taken back from its last contributing one, then the ray's set-up;
+ * the tile's gradient to its slot.  With a checkpoint every K > 1 steps each segment is recomputed from
+ * its kept state into a ring of K states and taken back from there; with K = 1 every state was kept and
+ * nothing is recomputed: each warp's kept states come through a ring of kStage steps in shared memory,
+ * copied there by cp.async kStage - 1 steps ahead of their use. */
+template <int kK> __global__ void __launch_bounds__(kThreads, 3) adjointReverse(const AdjointLaunch L) {
     __shared__ AdjointView v;
     copyView(L, v);
     __syncthreads();
@@ -898,59 +904,98 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointReverse(con
         const float4 bar = tr.bar[t.ray];
         const float sumBar[3] = {bar.x, bar.y, bar.z}, throughEnd = bar.w;
         const BackTerms bt = backTerms(a, c.step);
-        Kept ring[kK ? kK : kMaxK];
         StepBar next;
         memset(&next, 0, sizeof next);
         ConstBar g, gs; /* gs: what the steps' own maps give the constants the step length scales */
         memset(&g, 0, sizeof g);
         memset(&gs, 0, sizeof gs);
         float throughBar = 0.f, direct = 0.f; /* direct: velocities against what crossings add to their adjoints */
-        for (int first = ((top - 1) / K) * K; first >= 0; first -= K) {
-            const int last = min(first + K, top); /* steps first .. last - 1 */
-            /* the segment's states from its kept start; the state after its last step is the ray's end
-             * when that step was the ray's last, else one more step on */
-            RayState<float> r;
-            float through;
-            loadState(tr.saved + (size_t)(3 * (first / K)) * tr.rays + t.ray, tr.rays, r, through);
-            float junk[3] = {0.f, 0.f, 0.f};
-            unsigned n = 0;
-            for (int step = first; step < last; ++step) {
-                ring[step - first] = Kept{r, through};
-                if (step == steps - 1) break;
-                StepOut<float> o;
-                stepOnce(v, rhoScale, c, r, o, through, junk, n);
-                r = o.next;
+        RayState<float> after; /* the state after the step being taken back */
+        /* One step taken back: k, the state it started from; after, the state it ended in. */
+        auto back = [&](const Kept& k, int step) {
+            StepOut<float> o;
+            o.next = after;
+            o.k1 = bendAt(c, k.s.u);
+            accelWith(bt, c.big, k.s.n, o.a1);
+            StepBar b;
+            memset(&b, 0, sizeof b);
+            b.nextU = next.u;
+            for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
+            b.nextPsi = next.psi;
+            b.nextDrag = next.drag;
+            if (escaped && step == steps - 1 && f.stars > 0.f)
+                skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
+            Crossing<float> x;
+            const bool crossed = crossingOf(f, rhoScale, c, k.s, o, x);
+            if (crossed) {
+                crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
+                direct += k.s.w * b.w + k.s.v[0] * b.v[0] + k.s.v[1] * b.v[1] + k.s.v[2] * b.v[2];
             }
-            RayState<float> after = r;
-            if (last == steps) {
-                float unused;
-                loadState(tr.end + t.ray, tr.rays, after, unused);
-            }
-            for (int step = last - 1; step >= first; --step) {
-                const Kept k = ring[step - first];
-                StepOut<float> o;
-                o.next = after;
-                o.k1 = bendAt(c, k.s.u);
-                accelWith(bt, c.big, k.s.n, o.a1);
-                StepBar b;
-                memset(&b, 0, sizeof b);
-                b.nextU = next.u;
-                for (int j = 0; j < 3; ++j) b.nextN[j] = next.n[j];
-                b.nextPsi = next.psi;
-                b.nextDrag = next.drag;
-                if (escaped && step == steps - 1 && f.stars > 0.f)
-                    skyBack(v, c, k.s, o.next, throughEnd, sumBar, throughBar, b, g);
-                Crossing<float> x;
-                const bool crossed = crossingOf(f, rhoScale, c, k.s, o, x);
-                if (crossed) {
-                    crossingBack(v, rhoScale, c, k.s, o, x, k.through, sumBar, throughBar, b, g);
-                    direct += k.s.w * b.w + k.s.v[0] * b.v[0] + k.s.v[1] * b.v[1] + k.s.v[2] * b.v[2];
+            radialBack(bt, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, crossed, b.u, b.w,
+                       b.psi, b.drag, g, gs);
+            polarBack(bt, c.big, k.s.n, k.s.v, b.nextN, next.v, b.a1, crossed, b.n, b.v, g, gs);
+            next = b;
+            after = k.s;
+        };
+        float unused;
+        if constexpr (kK == 1) {
+            /* the state after the last step taken back: the ray's end when that step was its last, else kept */
+            loadState(top == steps ? tr.end + t.ray : tr.saved + (size_t)(3 * top) * tr.rays + t.ray, tr.rays, after,
+                      unused);
+            /* The warp walks back together from its highest step, each lane taking back only its own steps
+             * (below its top): at each step the active lanes' kept states are one run of 512 bytes in each
+             * of the trail's three planes. */
+            const int warpTop = __reduce_max_sync(__activemask(), top);
+            const float4* lane = tr.saved + t.ray;
+            __shared__ float4 stage[kThreads / 32][kStage][3][32];
+            float4(*mine)[3][32] = stage[threadIdx.x >> 5];
+            const int me = (int)(threadIdx.x & 31);
+            auto fetch = [&](int s) {
+                if (s >= 0 && s < top) {
+                    const float4* from = lane + (size_t)(3 * s) * tr.rays;
+                    for (int q = 0; q < 3; ++q) {
+                        const unsigned to = (unsigned)__cvta_generic_to_shared(&mine[s % kStage][q][me]);
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(to), "l"(from + q * tr.rays)
+                                     : "memory");
+                    }
                 }
-                radialBack(bt, c, k.s.u, k.s.w, k.s.drag, b.nextU, next.w, b.nextPsi, b.nextDrag, b.k1, crossed, b.u,
-                           b.w, b.psi, b.drag, g, gs);
-                polarBack(bt, c.big, k.s.n, k.s.v, b.nextN, next.v, b.a1, crossed, b.n, b.v, g, gs);
-                next = b;
-                after = k.s;
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+            };
+            for (int j = 0; j < kStage - 1; ++j) fetch(warpTop - 1 - j);
+            for (int step = warpTop - 1; step >= 0; --step) {
+                fetch(step - (kStage - 1)); /* into the slot the step before this one was read from */
+                asm volatile("cp.async.wait_group %0;\n" ::"n"(kStage - 1) : "memory");
+                if (step < top) {
+                    const float4(*at)[32] = mine[step % kStage];
+                    const float4 p0 = at[0][me], p1 = at[1][me], p2 = at[2][me];
+                    Kept k;
+                    k.s.u = p0.x, k.s.w = p0.y, k.s.n[0] = p0.z, k.s.n[1] = p0.w;
+                    k.s.n[2] = p1.x, k.s.v[0] = p1.y, k.s.v[1] = p1.z, k.s.v[2] = p1.w;
+                    k.s.psi = p2.x, k.s.drag = p2.y, k.through = p2.z;
+                    back(k, step);
+                }
+            }
+        } else {
+            Kept ring[kK ? kK : kMaxK];
+            for (int first = ((top - 1) / K) * K; first >= 0; first -= K) {
+                const int last = min(first + K, top); /* steps first .. last - 1 */
+                /* the segment's states from its kept start; the state after its last step is the ray's end
+                 * when that step was the ray's last, else one more step on */
+                RayState<float> r;
+                float through;
+                loadState(tr.saved + (size_t)(3 * (first / K)) * tr.rays + t.ray, tr.rays, r, through);
+                float junk[3] = {0.f, 0.f, 0.f};
+                unsigned n = 0;
+                for (int step = first; step < last; ++step) {
+                    ring[step - first] = Kept{r, through};
+                    if (step == steps - 1) break;
+                    StepOut<float> o;
+                    stepOnce(v, rhoScale, c, r, o, through, junk, n);
+                    r = o.next;
+                }
+                after = r;
+                if (last == steps) loadState(tr.end + t.ray, tr.rays, after, unused);
+                for (int step = last - 1; step >= first; --step) back(ring[step - first], step);
             }
         }
         /* The step length's adjoint from the motion, over the whole ray at once.  A Nystrom step of length h
@@ -1166,6 +1211,9 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     if (K == 32) {
         adjointForward<32><<<grid, kThreads, 0, stream>>>(L);
         adjointReverse<32><<<grid, kThreads, 0, stream>>>(L);
+    } else if (K == 1) {
+        adjointForward<1><<<grid, kThreads, 0, stream>>>(L);
+        adjointReverse<1><<<grid, kThreads, 0, stream>>>(L);
     } else {
         adjointForward<0><<<grid, kThreads, 0, stream>>>(L);
         adjointReverse<0><<<grid, kThreads, 0, stream>>>(L);

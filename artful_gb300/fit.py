@@ -104,9 +104,11 @@ def config5_fits(count: int = 32, seed: int = 3, stars: float = 1.0, offset=DRAW
 # ---- the adjoint through the C ABI -----------------------------------------------------------------------
 
 class Adjoint:
-    """artfCudaHoleAdjoint for views of one size: losses (n,), gradients (n, 5), the launch's stats."""
+    """artfCudaHoleAdjoint for views of one size: losses (n,), gradients (n, 5), the launch's stats.
+    checkpoint: the interval of the rays' kept states; 1 keeps every state (48 bytes a step, up to 192
+    steps a ray) and recomputes nothing, the fastest; 8 .. 64 keep less and recompute in between."""
 
-    def __init__(self, lib, ctx, width: int, height: int, map_ptr=None, fluid_ptr=None, checkpoint: int = 32):
+    def __init__(self, lib, ctx, width: int, height: int, map_ptr=None, fluid_ptr=None, checkpoint: int = 1):
         self.lib, self.ctx = lib, ctx
         self.width, self.height = width, height
         self.map_ptr, self.fluid_ptr = map_ptr, fluid_ptr

@@ -55,6 +55,9 @@ MIXED_PIPES_BUSY = {"fp64": 0.511, "fp32_fma": 0.317, "issue": 0.660,
                     "source": "ncu sm__inst_executed_pipe_fp64, sm__pipe_fma_cycles_active, smsp__issue_active "
                               "of traceMixedQueueOneAll at 960x540 x 4"}
 TRACE_TRAFFIC_SOURCE = "ncu dram__bytes of one launch of the mixed trace kernel at 1920x1080 x 4 jittered rays"
+# The adjoint's checkpoint interval: 32, a ray's state kept every 32 steps and each segment recomputed in
+# the reverse pass; 1, every state kept (48 bytes a step) and nothing recomputed.
+ADJOINT_CHECKPOINT = 1
 
 
 def parse():
@@ -70,6 +73,8 @@ def parse():
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--views", type=int, default=1, help="views of --profile adjoint")
+    p.add_argument("--checkpoint", type=int, default=ADJOINT_CHECKPOINT,
+                   help="checkpoint interval of --profile adjoint (1: every state kept)")
     p.add_argument("--guards", type=int, default=0,
                    help="the mixed trace's FP64 guards for --profile mixed (ARTF_CUDA_GUARD_* bits; 0: all)")
     p.add_argument("--persistent", action="store_true", help="the persistent form of --profile exact/fp32/fp64")
@@ -106,7 +111,7 @@ def gradient_bias(args):
     unit = scenes.unit_fluid()
     capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 0))
     w, h = 256, 144
-    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=ADJOINT_CHECKPOINT)
     targets = adj.render([t for t, _ in fits])
     fp64 = fit.Fp64Loss(lib, ctx, w, h, m, lib.artfCudaDeviceFluid(ctx), 10 * len(fits))
 
@@ -320,12 +325,12 @@ def profile_case(args):
         capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 1))
         unit = scenes.unit_fluid()
         capi.check(lib.artfCudaSetFluid(ctx, unit.ctypes.data, 1))
-        adj = fit.Adjoint(lib, ctx, args.width, args.height, checkpoint=32)
+        adj = fit.Adjoint(lib, ctx, args.width, args.height, checkpoint=args.checkpoint)
         targets = adj.render([target] * args.views)
         for _ in range(2):
             loss, grad, s = adj([start] * args.views, targets)
         print(json.dumps({"profile": "adjoint", "width": args.width, "height": args.height, "views": args.views,
-                          "ms": s.ms, "rays": s.rays, "steps": s.steps, "grad": grad[0].tolist()}))
+                          "checkpoint": args.checkpoint, "ms": s.ms, "rays": s.rays, "steps": s.steps, "grad": grad[0].tolist()}))
         lib.artfCudaDestroy(ctx)
         return
     scene = scenes.config2(4)
@@ -758,23 +763,24 @@ def _median_ms(run, steps, flush=None):
 
 def adjoint_measurement(lib, ctx, steps, flush):
     """Configuration 4: the adjoint at 512 x 288 (a = 0.6, i = 55 deg, r_in = 1.1 r_ISCO, q = 2.7,
-    r_obs = 32 against the image of a = 0.7, i = 60 deg, r_in = r_ISCO, q = 3, r_obs = 30), checkpoints
-    every 32 steps, beside the forward traces of the same rays (FP32 and mixed precision); and eight such
-    views in one adjoint launch beside one forward trace of as many pixels."""
+    r_obs = 32 against the image of a = 0.7, i = 60 deg, r_in = r_ISCO, q = 3, r_obs = 30), with its
+    checkpoint interval (ADJOINT_CHECKPOINT), beside the forward traces of the same rays (FP32 and mixed
+    precision); eight such views in one adjoint launch beside one forward trace of as many pixels; and
+    both again with the other interval (every state kept, or a checkpoint every 32 steps)."""
     import torch
     from artful_gb300 import capi, fit
     target, start = fit.config4_params()
     m = fit.param_map(start)
     capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
     w, h = 512, 288
-    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=ADJOINT_CHECKPOINT)
     targets = adj.render([target])
     torch.cuda.synchronize()
     last = {}
 
-    def run_adjoint(views, tg):
+    def run_adjoint(views, tg, k=ADJOINT_CHECKPOINT):
         def go():
-            loss, grad, st = adj(views, tg)
+            loss, grad, st = adj(views, tg, checkpoint=k)
             last.update(loss=loss, grad=grad, stats=st)
             return st.ms
         return go
@@ -800,8 +806,13 @@ def adjoint_measurement(lib, ctx, steps, flush):
     ms_adj8 = _median_ms(run_adjoint([start] * 8, eight), steps, flush)
     steps8 = last["stats"].steps
     ms_fp32_big = _median_ms(run_forward(start, 1448, 816, capi.FP32), steps, flush)
+    other = 32 if ADJOINT_CHECKPOINT == 1 else 1
+    ms_other = _median_ms(run_adjoint([start], targets, other), steps, flush)
+    grad_other = last["grad"][0]
+    ms_other8 = _median_ms(run_adjoint([start] * 8, eight, other), steps, flush)
     return {
-        "workload": "512x288, 1 ray at each pixel centre, loss = MSE of linear RGB against the target's image, K=32",
+        "workload": "512x288, 1 ray at each pixel centre, loss = MSE of linear RGB against the target's image, "
+                    f"K={ADJOINT_CHECKPOINT}" + (" (every state kept)" if ADJOINT_CHECKPOINT == 1 else ""),
         "adjoint_ms": ms_adj, "forward_fp32_ms": ms_fp32, "forward_mixed_ms": ms_mixed,
         "adjoint_over_forward_fp32": ms_adj / ms_fp32, "adjoint_over_forward_mixed": ms_adj / ms_mixed,
         "steps": one["stats"].steps, "loss": float(one["loss"][0]),
@@ -809,6 +820,10 @@ def adjoint_measurement(lib, ctx, steps, flush):
         "batched_8_views": {"adjoint_ms": ms_adj8, "steps": steps8,
                             "forward_fp32_1448x816_ms": ms_fp32_big,
                             "adjoint_over_forward_fp32": ms_adj8 / ms_fp32_big},
+        "other_checkpoint": {"checkpoint": other, "adjoint_ms": ms_other, "adjoint_over_forward_fp32": ms_other / ms_fp32,
+                             "batched_8_views_ms": ms_other8, "batched_8_over_forward_fp32": ms_other8 / ms_fp32_big,
+                             "gradient_max_rel_diff": float(np.max(np.abs(grad_other - one["grad"][0]))
+                                                            / np.max(np.abs(one["grad"][0])))},
     }
 
 
@@ -958,7 +973,7 @@ def fit_measurement(lib, ctx, fd_fits):
     m = fit.param_map(fits[0][0])
     capi.check(lib.artfCudaSetMap(ctx, m.ctypes.data, 0))
     w, h = 256, 144
-    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=ADJOINT_CHECKPOINT)
     fit.fit_batch(adj, fits[:2], steps=3)  # warm-up
     theta, history, wall = fit.fit_batch(adj, fits, steps=200, lr=1e-2)
     err = fit.recovery_error(theta, fits)
@@ -971,7 +986,8 @@ def fit_measurement(lib, ctx, fd_fits):
                 "fits_within_5pct": int((e.max(1) < 0.05).sum()), "fits_within_10pct": int((e.max(1) < 0.10).sum())}
 
     out = {"workload": "32 fits of 256x144, spin, inclination and inner radius started 15% off and fitted "
-                       "(q = 3, r_obs = 30 held), 200 Adam steps, lr 1e-2 (relative to the start), adjoint K=32",
+                       "(q = 3, r_obs = 30 held), 200 Adam steps, lr 1e-2 (relative to the start), "
+                       f"adjoint K={ADJOINT_CHECKPOINT}",
            "wall_s": wall, "wall_per_fit_s": wall / len(fits), "start_error": 0.15,
            "loss_first_last": [float(history[0]), float(history[-1])], "recovery_error": summary(err)}
     # why: the adjoint's gradient against finite differences of its own forward renders, pixel by pixel,

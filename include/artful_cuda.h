@@ -400,7 +400,7 @@ int artfCudaHoleTangents(ArtfCuda* ctx, const ArtfCudaHoleParams* params, const 
                          const ArtfCudaHoleFrame64* frame64, const double* jacobian, const float* map,
                          const float* fluid, double* out);
 
-#define ARTF_CUDA_ADJOINT_MIN_CHECKPOINT 8
+#define ARTF_CUDA_ADJOINT_MIN_CHECKPOINT 1
 #define ARTF_CUDA_ADJOINT_MAX_CHECKPOINT 64
 #define ARTF_CUDA_ADJOINT_MAX_VIEWS 1024
 
@@ -413,7 +413,7 @@ typedef struct ArtfCudaAdjointResult {
 
 /* The adjoint: reverse-mode derivatives of the FP32 trace, checkpointing the ray's state every
  * `checkpointEvery` steps (ARTF_CUDA_ADJOINT_MIN_CHECKPOINT .. ARTF_CUDA_ADJOINT_MAX_CHECKPOINT) and
- * recomputing in between.  `count` views (params[0 .. count - 1]) of one size, one ray at each pixel's
+ * recomputing in between; 1 keeps every state (up to 192 a ray, 48 bytes each) and recomputes nothing.  `count` views (params[0 .. count - 1]) of one size, one ray at each pixel's
  * centre, in one launch.  The rings' orbit speed and glow come from their formulas; the map's other
  * tables (gas, dust, sky, colours) and the fluid are shared by the views: device pointers (NULL: the
  * context's).  targets: device, count * width * height float4 (linear RGB, the fourth unused).  hdr:

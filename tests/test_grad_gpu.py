@@ -154,9 +154,10 @@ def test_adjoint_matches_forward_mode(lib, ctx, torch, scene, w, h):
     assert np.all(err <= 2e-2 * np.abs(grad64) + 5e-3 * np.abs(grad64).max()), (grad[0], grad64)
 
 
-def test_adjoint_workload_per_pixel(lib, ctx, torch, scene):
-    """The adjoint workload (512 x 288, checkpoints every 32 steps): loss between the start and the
-    target's image.  Each pixel's share of the gradient against the forward-mode reference's: where the
+@pytest.mark.parametrize("k", [1, 32])
+def test_adjoint_workload_per_pixel(lib, ctx, torch, scene, k):
+    """The adjoint workload (512 x 288; every state kept, or checkpoints every 32 steps): loss between
+    the start and the target's image.  Each pixel's share of the gradient against the forward-mode reference's: where the
     FP32 ray and the FP64 ray make the same choices (their radiance agrees within 1e-3), at least 99% of the
     shares that carry weight agree within 2%, and those pixels' sums within 0.5% of the gradient's largest
     component.  The few pixels where FP32 and FP64 choose differently (another star cell, a crossing
@@ -168,7 +169,7 @@ def test_adjoint_workload_per_pixel(lib, ctx, torch, scene):
     loss64, grad64 = _loss_and_grad_from_tangents(tan, target)
     hdr = torch.zeros((1, h, w, 4), dtype=torch.float32, device="cuda")
     shares = torch.zeros((1, h, w, 5), dtype=torch.float32, device="cuda")
-    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=32)
+    adj = fit.Adjoint(lib, ctx, w, h, checkpoint=k)
     loss, grad, _ = adj([start], torch.from_numpy(_rgba(target)[None]).cuda(), hdr, pixel_grads=shares)
     assert loss[0] == pytest.approx(loss64, rel=2e-3)
     value = tan[..., 0]
@@ -191,12 +192,13 @@ def test_adjoint_workload_per_pixel(lib, ctx, torch, scene):
 
 
 def test_adjoint_invariances(lib, ctx, torch, scene):
-    """The checkpoint interval changes what is recomputed, not the result; a view's result does not depend
-    on the views batched with it; the same call gives the same bits."""
+    """The checkpoint interval changes what is recomputed, not the result (1: every state kept, nothing
+    recomputed); a view's result does not depend on the views batched with it; the same call gives the
+    same bits."""
     target_p, start = scene
     target = _rgba(_tangents(lib, ctx, torch, target_p, W, H)[..., 0])
     base = _adjoint(lib, ctx, torch, [start], target[None], W, H, k=32)
-    for k in (8, 16, 64):
+    for k in (1, 8, 16, 64):
         other = _adjoint(lib, ctx, torch, [start], target[None], W, H, k=k)
         assert other[0][0] == base[0][0]
         np.testing.assert_allclose(other[1], base[1], rtol=1e-5, atol=1e-7 * np.abs(base[1]).max())
@@ -226,7 +228,7 @@ def test_adjoint_rejects_bad_arguments(lib, ctx, torch, scene):
     res = (capi.AdjointResult * 2)()
     arr = (capi.HoleParams * 2)(start, start)
     # (a count above the limit is refused before params is read)
-    for n, k in ((1, 7), (1, 65), (0, 32), (capi.ADJOINT_MAX_VIEWS + 1, 32)):
+    for n, k in ((1, 0), (1, 65), (0, 32), (capi.ADJOINT_MAX_VIEWS + 1, 32)):
         assert lib.artfCudaHoleAdjoint(ctx, arr, n, W, H, None, None, t.data_ptr(), k, None, None, res, None) == -1
     assert lib.artfCudaHoleAdjoint(ctx, arr, 1, W, H, None, None, None, 32, None, None, res, None) == -1
     assert lib.artfCudaHoleAdjoint(ctx, arr, 1, 0, H, None, None, t.data_ptr(), 32, None, None, res, None) == -1
