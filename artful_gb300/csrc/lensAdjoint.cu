@@ -53,6 +53,8 @@ constexpr int kMaxK = ARTF_CUDA_ADJOINT_MAX_CHECKPOINT;
 /* With every state kept: the steps a warp's reads run ahead of its step back, through shared memory. */
 constexpr int kStage = 4;
 constexpr int kMaxSteps = 192;
+constexpr int kAdjointClasses = kMaxSteps / 8 + 1; /* a tile's weight: its steps / 8 */
+constexpr int kClassStride = 32;                   /* a view's class counters */
 constexpr float kTurn = .15915494f; /* 1 / 2 pi, the reference's constant */
 
 /* Adjoints of what a ray's constants of motion and the frame's scalars feed. */
@@ -751,7 +753,9 @@ struct AdjointLaunch {
     const AdjointView* views;
     float* partials; /* 8 floats a tile: the loss, the five gradient components, two unused */
     unsigned long long* counters;
-    const int* order; /* each view's tiles, heaviest first (tilesPerView a view), or NULL: in order */
+    const int* order;  /* each view's tiles for the reverse kernel, heaviest first (tilesPerView a view) */
+    int* weights;      /* each tile's weight for that order, and each view's count of tiles a weight, */
+    unsigned* classes; /* both written by the forward kernel */
     Trail trail;
     int tilesX, tilesPerView, totalTiles, K;
 };
@@ -788,11 +792,11 @@ struct TileLane {
     bool inside;
 };
 
-__device__ __forceinline__ bool tileLane(const AdjointLaunch& L, const AdjointView& v, TileLane& t) {
+__device__ __forceinline__ bool tileLane(const AdjointLaunch& L, const int* order, const AdjointView& v, TileLane& t) {
     const int lane = (int)(threadIdx.x & 31);
     const int slot = (int)(blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5));
     if (slot >= L.tilesPerView) return false; /* the whole warp: its tile lies past the view */
-    t.local = L.order ? L.order[(size_t)blockIdx.y * L.tilesPerView + slot] : slot;
+    t.local = order ? order[(size_t)blockIdx.y * L.tilesPerView + slot] : slot;
     t.px = (t.local % L.tilesX) * 8 + (lane & 7), t.py = (t.local / L.tilesX) * 4 + (lane >> 3);
     t.tile = (size_t)blockIdx.y * L.tilesPerView + t.local;
     t.ray = t.tile * 32 + (size_t)lane;
@@ -809,15 +813,16 @@ __device__ __forceinline__ void copyView(const AdjointLaunch& L, AdjointView& v)
 /* The forward kernel: each ray traced with its shading, the state kept at the start of every segment of K
  * steps, the loss and its adjoint in the radiance; the tile's loss to its slot.  kK: the checkpoint
  * interval as a constant (the default, 32: segment indices are shifts), or 0 to read it from L. */
-template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(const AdjointLaunch L) {
+template <int kK> __global__ void __launch_bounds__(kThreads, 6) adjointForward(const AdjointLaunch L) {
     __shared__ AdjointView v;
     copyView(L, v);
     __syncthreads();
     TileLane t;
-    if (!tileLane(L, v, t)) return;
+    if (!tileLane(L, nullptr, v, t)) return;
     const int K = kK ? kK : L.K;
     const Trail& tr = L.trail;
     float loss = 0.f;
+    int top = 0;
     Tally tally;
     if (t.inside) {
         const Frame<float>& f = v.f;
@@ -859,7 +864,7 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(con
          * last disc crossing): after it every adjoint is zero, and a step taken back with zero adjoints
          * adds exactly nothing, so those steps, and the recomputation of segments holding only them, are
          * skipped. */
-        const int top = escaped && f.stars > 0.f ? steps : lastCrossing + 1;
+        top = escaped && f.stars > 0.f ? steps : lastCrossing + 1;
         tr.head[t.ray] = make_int4(steps, top, escaped ? 1 : 0, 0);
         tr.bar[t.ray] = make_float4(2.f * diff[0] * v.lossScale, 2.f * diff[1] * v.lossScale,
                                     2.f * diff[2] * v.lossScale, through);
@@ -873,7 +878,14 @@ template <int kK> __global__ void __launch_bounds__(kThreads) adjointForward(con
     }
     flushTally(tally, L.counters);
     for (int off = 16; off > 0; off >>= 1) loss += __shfl_down_sync(0xFFFFFFFFu, loss, off);
-    if ((threadIdx.x & 31) == 0) L.partials[t.tile * 8] = loss;
+    /* the tile's weight in the reverse kernel's order: the most steps one of its rays takes back */
+    const int most = __reduce_max_sync(0xFFFFFFFFu, top);
+    if ((threadIdx.x & 31) == 0) {
+        L.partials[t.tile * 8] = loss;
+        const int w = min(most >> 3, kAdjointClasses - 1);
+        L.weights[t.tile] = w;
+        atomicAdd(L.classes + blockIdx.y * kClassStride + w, 1u);
+    }
 }
 
 /* The reverse kernel: each ray's steps taken back from its last contributing one, then the ray's set-up;
@@ -886,7 +898,7 @@ template <int kK> __global__ void __launch_bounds__(kThreads, 3) adjointReverse(
     copyView(L, v);
     __syncthreads();
     TileLane t;
-    if (!tileLane(L, v, t)) return;
+    if (!tileLane(L, L.order, v, t)) return;
     const int K = kK ? kK : L.K;
     const Trail& tr = L.trail;
     float grad[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1022,46 +1034,13 @@ template <int kK> __global__ void __launch_bounds__(kThreads, 3) adjointReverse(
 }
 
 /* ---- heavy tiles first ----------------------------------------------------------------------------
- * Blocks are dispatched in order and a ray's adjoint costs in proportion to its steps, so the heaviest
- * tiles go to the first blocks: the launch does not end on a few photon-ring tiles while the rest of the
- * GPU idles.  A tile's weight is the step count of one FP32 ray through its middle, up to 64 steps, in
- * classes of 8; a counting sort a view orders the tiles.  Each tile still writes its own partial sums and
- * adjointSums adds them in tile order, so the gradients are the same bits in any order. */
-constexpr int kAdjointClasses = 9;
-constexpr int kClassStride = 16; /* a view's class counters */
-
-__global__ void __launch_bounds__(128) adjointProbe(const AdjointLaunch L, int* weights, unsigned* classes) {
-    __shared__ unsigned counts[kAdjointClasses];
-    if (threadIdx.x < kAdjointClasses) counts[threadIdx.x] = 0;
-    __syncthreads();
-    const int local = (int)(blockIdx.x * 128 + threadIdx.x);
-    if (local < L.tilesPerView) {
-        const AdjointView& v = L.views[blockIdx.y];
-        const int px = min((local % L.tilesX) * 8 + 4, v.f.width - 1);
-        const int py = min((local / L.tilesX) * 4 + 2, v.f.height - 1);
-        float nx, ny, moment;
-        samplePosition(v.h, 0, 0, px, py, 0, &nx, &ny, &moment);
-        RayConst<float> c;
-        RayState<float> s;
-        rayStart(v.f, nx, ny, v.h.disc[2] + v.h.spin[3] * moment, 1.f, c, s);
-        const float a = v.f.a;
-        if (a != 0.f) s.drag = dragAt(a, a * a, c.xiA, s.u);
-        int i = 0;
-        while (i < 64) {
-            StepOut<float> o;
-            nystromStep(a, c, s, o);
-            ++i;
-            if (0.f > o.next.u || o.next.u > v.f.uHorizon) break;
-            s = o.next;
-        }
-        const int w = min(i >> 3, kAdjointClasses - 1);
-        weights[(size_t)blockIdx.y * L.tilesPerView + local] = w;
-        atomicAdd(counts + w, 1u);
-    }
-    __syncthreads();
-    if (threadIdx.x < kAdjointClasses && counts[threadIdx.x])
-        atomicAdd(classes + blockIdx.y * kClassStride + threadIdx.x, counts[threadIdx.x]);
-}
+ * Blocks are dispatched in order and a ray's step back costs in proportion to its steps, so the reverse
+ * kernel's heaviest tiles go to its first blocks: the launch does not end on a few photon-ring tiles
+ * while the rest of the GPU idles.  A tile's weight is what the forward kernel found, the most steps a ray
+ * of the tile takes back, in classes of 8 up to 192; a counting sort a view orders the tiles.  (The
+ * forward kernel runs in tile order: ordering it too, by a probe ray a tile, cost more than it saved.)
+ * Each tile still writes its own partial sums and adjointSums adds them in tile order, so the gradients
+ * are the same bits in any order. */
 
 __global__ void __launch_bounds__(128) adjointPlace(const AdjointLaunch L, const int* weights, const unsigned* classes,
                                                     unsigned* cursors, int* order) {
@@ -1093,10 +1072,24 @@ __global__ void __launch_bounds__(128) adjointPlace(const AdjointLaunch L, const
  * takes a run of the view's tiles (thread t adds the run's tiles t, t + 256, ... in turn, then a tree over
  * the threads, the six sums of a tile read together), and the view's last block to finish (a ticket a
  * view, zeroed before the launch) adds the blocks' sums in block order. */
-constexpr int kSumBlocks = 64;
+constexpr int kSumBlocks = 64; /* a power of two */
 
+/* Adds part[k][0 .. 2 half - 1] into part[k][0], pairwise in a fixed order. */
+__device__ __forceinline__ void treeSum(double (*part)[256], int half) {
+    for (int width = half; width > 0; width >>= 1) {
+        if ((int)threadIdx.x < width)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + width];
+        __syncthreads();
+    }
+}
+
+/* Each view's six sums, in double and in a fixed order: kSumBlocks blocks a view, each adding a run of
+ * the view's tiles; the last block of the view to finish (a ticket) adds the blocks' sums, read at once
+ * and added pairwise. */
 __global__ void __launch_bounds__(256) adjointSums(const float* partials, int tilesPerView, double* blockSums,
                                                    unsigned* tickets, double* results) {
+    static_assert(kSumBlocks <= 256, "a thread a block's sums in the last pass");
     __shared__ double part[6][256];
     __shared__ unsigned ticket;
     const int view = (int)blockIdx.y, run = (tilesPerView + kSumBlocks - 1) / kSumBlocks;
@@ -1111,12 +1104,7 @@ __global__ void __launch_bounds__(256) adjointSums(const float* partials, int ti
 #pragma unroll
     for (int k = 0; k < 6; ++k) part[k][threadIdx.x] = s[k];
     __syncthreads();
-    for (int width = 128; width > 0; width >>= 1) {
-        if ((int)threadIdx.x < width)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + width];
-        __syncthreads();
-    }
+    treeSum(part, 128);
     double* sums = blockSums + (size_t)view * kSumBlocks * 8;
     if (threadIdx.x < 6) sums[blockIdx.x * 8 + threadIdx.x] = part[threadIdx.x][0];
     __threadfence();
@@ -1125,11 +1113,12 @@ __global__ void __launch_bounds__(256) adjointSums(const float* partials, int ti
     __syncthreads();
     if (ticket != kSumBlocks - 1) return;
     __threadfence();
-    if (threadIdx.x < 6) {
-        double total = 0.0;
-        for (int b = 0; b < kSumBlocks; ++b) total += __ldcg(sums + b * 8 + threadIdx.x);
-        results[(size_t)view * 8 + threadIdx.x] = total;
-    }
+    if ((int)threadIdx.x < kSumBlocks)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) part[k][threadIdx.x] = __ldcg(sums + threadIdx.x * 8 + k);
+    __syncthreads();
+    treeSum(part, kSumBlocks / 2);
+    if (threadIdx.x < 6) results[(size_t)view * 8 + threadIdx.x] = part[threadIdx.x][0];
 }
 
 }  // namespace
@@ -1182,7 +1171,6 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.views = (const AdjointView*)table;
     L.partials = partials;
     L.counters = counters;
-    L.order = nullptr;
     L.tilesX = (width + 7) / 8;
     L.tilesPerView = adjointTiles(width, height);
     L.totalTiles = L.tilesPerView * count;
@@ -1193,31 +1181,36 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.trail.end = L.trail.bar + L.trail.rays;
     L.trail.saved = L.trail.end + 3 * L.trail.rays;
     if (!orderScratch) return cudaErrorInvalidValue; /* (it holds the sums' tickets and blocks too) */
+    const size_t tiles = (size_t)count * L.tilesPerView;
     unsigned* classes = (unsigned*)orderScratch;
     unsigned* cursors = classes + kClassStride * (size_t)count;
     unsigned* tickets = cursors + kClassStride * (size_t)count;
     int* weights = (int*)(tickets + count);
-    int* order = weights + (size_t)count * L.tilesPerView;
-    const size_t ints = orderHead(count) + sizeof(int) * 2 * (size_t)count * L.tilesPerView;
+    int* order = weights + tiles;
+    const size_t ints = orderHead(count) + sizeof(int) * 2 * tiles;
     double* blockSums = (double*)((char*)orderScratch + (ints + 15) / 16 * 16);
     const cudaError_t e = cudaMemsetAsync(orderScratch, 0, orderHead(count), stream);
     if (e != cudaSuccess) return e;
-    const dim3 probeGrid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
-    adjointProbe<<<probeGrid, 128, 0, stream>>>(L, weights, classes);
-    adjointPlace<<<probeGrid, 128, 0, stream>>>(L, weights, classes, cursors, order);
+    const dim3 placeGrid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
     L.order = order;
+    L.weights = weights;
+    L.classes = classes;
     const unsigned blocks = (unsigned)((L.tilesPerView + kThreads / 32 - 1) / (kThreads / 32));
     const dim3 grid(blocks, (unsigned)count);
-    if (K == 32) {
+    /* the forward kernel, the reverse kernel's order from what it found, the reverse kernel */
+    if (K == 32)
         adjointForward<32><<<grid, kThreads, 0, stream>>>(L);
-        adjointReverse<32><<<grid, kThreads, 0, stream>>>(L);
-    } else if (K == 1) {
+    else if (K == 1)
         adjointForward<1><<<grid, kThreads, 0, stream>>>(L);
-        adjointReverse<1><<<grid, kThreads, 0, stream>>>(L);
-    } else {
+    else
         adjointForward<0><<<grid, kThreads, 0, stream>>>(L);
+    adjointPlace<<<placeGrid, 128, 0, stream>>>(L, weights, classes, cursors, order);
+    if (K == 32)
+        adjointReverse<32><<<grid, kThreads, 0, stream>>>(L);
+    else if (K == 1)
+        adjointReverse<1><<<grid, kThreads, 0, stream>>>(L);
+    else
         adjointReverse<0><<<grid, kThreads, 0, stream>>>(L);
-    }
     adjointSums<<<dim3(kSumBlocks, (unsigned)count), 256, 0, stream>>>(partials, L.tilesPerView, blockSums, tickets,
                                                                       results);
     return cudaGetLastError();
