@@ -1068,57 +1068,61 @@ __global__ void __launch_bounds__(128) adjointPlace(const AdjointLaunch L, const
     if (active) order[(size_t)blockIdx.y * L.tilesPerView + runs[w] + within] = local;
 }
 
-/* A view's tiles' sums in double, in a fixed order whatever the scheduling: each of kSumBlocks blocks
- * takes a run of the view's tiles (thread t adds the run's tiles t, t + 256, ... in turn, then a tree over
- * the threads, the six sums of a tile read together), and the view's last block to finish (a ticket a
- * view, zeroed before the launch) adds the blocks' sums in block order. */
-constexpr int kSumBlocks = 64; /* a power of two */
-
-/* Adds part[k][0 .. 2 half - 1] into part[k][0], pairwise in a fixed order. */
-__device__ __forceinline__ void treeSum(double (*part)[256], int half) {
-    for (int width = half; width > 0; width >>= 1) {
-        if ((int)threadIdx.x < width)
-#pragma unroll
-            for (int k = 0; k < 6; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + width];
-        __syncthreads();
-    }
+/* Knuth's TwoSum: s + e equals a + b exactly (no products, so no contraction applies). */
+__device__ __forceinline__ void twoSum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
 }
 
-/* Each view's six sums, in double and in a fixed order: kSumBlocks blocks a view, each adding a run of
- * the view's tiles; the last block of the view to finish (a ticket) adds the blocks' sums, read at once
- * and added pairwise. */
-__global__ void __launch_bounds__(256) adjointSums(const float* partials, int tilesPerView, double* blockSums,
-                                                   unsigned* tickets, double* results) {
-    static_assert(kSumBlocks <= 256, "a thread a block's sums in the last pass");
-    __shared__ double part[6][256];
-    __shared__ unsigned ticket;
-    const int view = (int)blockIdx.y, run = (tilesPerView + kSumBlocks - 1) / kSumBlocks;
-    const int begin = (int)blockIdx.x * run, end = min(begin + run, tilesPerView);
+/* A sum kept as an unevaluated pair hi + lo of floats: hi + lo += h + l, renormalised. */
+__device__ __forceinline__ void addPair(float& hi, float& lo, float h, float l) {
+    float s, e;
+    twoSum(hi, h, s, e);
+    e += lo + l;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+
+/* Each view's six sums in a fixed order: a block a view, each thread adding a stride of the view's tiles,
+ * then the threads' sums pairwise within each warp and the warps' in turn.  Every sum is a pair of floats
+ * (hi + lo, about 48 bits), so the float pipe does the work that double would give on this GPU's narrow
+ * FP64 pipe, and the result does not depend on scheduling. */
+__global__ void __launch_bounds__(1024) adjointSums(const float* partials, int tilesPerView, double* results) {
+    __shared__ float part[32][6][2];
+    const int view = (int)blockIdx.x, lane = (int)(threadIdx.x & 31), warp = (int)(threadIdx.x >> 5);
     const float4* mine = reinterpret_cast<const float4*>(partials + (size_t)view * tilesPerView * 8);
-    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int b = begin + (int)threadIdx.x; b < end; b += 256) {
-        const float4 lo = mine[(size_t)b * 2], hi = mine[(size_t)b * 2 + 1];
-        s[0] += (double)lo.x, s[1] += (double)lo.y, s[2] += (double)lo.z, s[3] += (double)lo.w;
-        s[4] += (double)hi.x, s[5] += (double)hi.y;
+    float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int b = (int)threadIdx.x; b < tilesPerView; b += 1024) {
+        const float4 x = mine[(size_t)b * 2], y = mine[(size_t)b * 2 + 1];
+        const float v[6] = {x.x, x.y, x.z, x.w, y.x, y.y};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) addPair(hi[k], lo[k], v[k], 0.f);
     }
+    for (int round = 0; round < 2; ++round) {
+        for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) part[k][threadIdx.x] = s[k];
-    __syncthreads();
-    treeSum(part, 128);
-    double* sums = blockSums + (size_t)view * kSumBlocks * 8;
-    if (threadIdx.x < 6) sums[blockIdx.x * 8 + threadIdx.x] = part[threadIdx.x][0];
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) ticket = atomicAdd(tickets + view, 1u);
-    __syncthreads();
-    if (ticket != kSumBlocks - 1) return;
-    __threadfence();
-    if ((int)threadIdx.x < kSumBlocks)
+            for (int k = 0; k < 6; ++k) {
+                const float h = __shfl_down_sync(0xFFFFFFFFu, hi[k], off);
+                const float l = __shfl_down_sync(0xFFFFFFFFu, lo[k], off);
+                addPair(hi[k], lo[k], h, l);
+            }
+        if (round == 1) break;
+        if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) part[k][threadIdx.x] = __ldcg(sums + threadIdx.x * 8 + k);
-    __syncthreads();
-    treeSum(part, kSumBlocks / 2);
-    if (threadIdx.x < 6) results[(size_t)view * 8 + threadIdx.x] = part[threadIdx.x][0];
+            for (int k = 0; k < 6; ++k) part[warp][k][0] = hi[k], part[warp][k][1] = lo[k];
+        __syncthreads();
+        if (warp != 0) return;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const bool held = lane < (int)(blockDim.x >> 5);
+            hi[k] = held ? part[lane][k][0] : 0.f, lo[k] = held ? part[lane][k][1] : 0.f;
+        }
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) results[(size_t)view * 8 + k] = (double)hi[k] + (double)lo[k];
 }
 
 }  // namespace
@@ -1147,13 +1151,12 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
     memcpy(slot, &v, sizeof v);
 }
 
-/* The order's scratch: class counts, cursors and the sums' tickets (zeroed before each launch), the
- * tiles' weights and order, then the sums' blocks (doubles). */
-static size_t orderHead(int count) { return sizeof(unsigned) * (2 * kClassStride + 1) * (size_t)count; }
+/* The order's scratch: class counts and cursors (zeroed before each launch), then the tiles' weights and
+ * order. */
+static size_t orderHead(int count) { return sizeof(unsigned) * 2 * kClassStride * (size_t)count; }
 
 size_t adjointOrderBytes(int count, int width, int height) {
-    const size_t ints = orderHead(count) + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
-    return (ints + 15) / 16 * 16 + sizeof(double) * 8 * kSumBlocks * (size_t)count;
+    return orderHead(count) + sizeof(int) * 2 * (size_t)count * adjointTiles(width, height);
 }
 
 /* The trail's rays: 32 a tile, padding lanes included. */
@@ -1180,15 +1183,12 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
     L.trail.bar = (float4*)(L.trail.head + L.trail.rays);
     L.trail.end = L.trail.bar + L.trail.rays;
     L.trail.saved = L.trail.end + 3 * L.trail.rays;
-    if (!orderScratch) return cudaErrorInvalidValue; /* (it holds the sums' tickets and blocks too) */
+    if (!orderScratch) return cudaErrorInvalidValue;
     const size_t tiles = (size_t)count * L.tilesPerView;
     unsigned* classes = (unsigned*)orderScratch;
     unsigned* cursors = classes + kClassStride * (size_t)count;
-    unsigned* tickets = cursors + kClassStride * (size_t)count;
-    int* weights = (int*)(tickets + count);
+    int* weights = (int*)(cursors + kClassStride * (size_t)count);
     int* order = weights + tiles;
-    const size_t ints = orderHead(count) + sizeof(int) * 2 * tiles;
-    double* blockSums = (double*)((char*)orderScratch + (ints + 15) / 16 * 16);
     const cudaError_t e = cudaMemsetAsync(orderScratch, 0, orderHead(count), stream);
     if (e != cudaSuccess) return e;
     const dim3 placeGrid((unsigned)((L.tilesPerView + 127) / 128), (unsigned)count);
@@ -1211,8 +1211,7 @@ cudaError_t launchAdjoint(const void* table, int count, int width, int height, i
         adjointReverse<1><<<grid, kThreads, 0, stream>>>(L);
     else
         adjointReverse<0><<<grid, kThreads, 0, stream>>>(L);
-    adjointSums<<<dim3(kSumBlocks, (unsigned)count), 256, 0, stream>>>(partials, L.tilesPerView, blockSums, tickets,
-                                                                      results);
+    adjointSums<<<(unsigned)count, 1024, 0, stream>>>(partials, L.tilesPerView, results);
     return cudaGetLastError();
 }
 

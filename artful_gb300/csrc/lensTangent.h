@@ -37,8 +37,8 @@ void adjointFillView(void* slot, const ArtfCudaHoleFrame& frame, const double* j
 cudaError_t launchAdjoint(const void* table, int count, int width, int height, int K, unsigned long long* counters,
                           float* partials, double* results, cudaStream_t stream, void* orderScratch, void* trail);
 size_t adjointTrailBytes(int count, int width, int height, int K);
-/* Device bytes of the adjoint's order scratch (orderScratch above, required): the heavy-first tile order
- * and the gradient sums' blocks and tickets. */
+/* Device bytes of the adjoint's order scratch (orderScratch above, required): the reverse kernel's
+ * heavy-first tile order, with the weights and class counts it is sorted from. */
 size_t adjointOrderBytes(int count, int width, int height);
 
 }  // namespace artf
