@@ -11,6 +11,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libartful_cuda.so")
 DEBUG_LIB_PATH = os.path.join(HERE, "libartful_cuda_debug.so")  # the bounds-checked build (build --debug)
+ENOMEM = -3
 EBOUNDS = -7
 
 MAP_WIDTH, MAP_HEIGHT = 2048, 1024

@@ -120,7 +120,14 @@ extern "C" int artfCudaFailAllocAfter(ArtfCuda* ctx, int allocations) {
 static cudaError_t ctxAlloc(ArtfCuda* ctx, void** p, size_t bytes, bool pageLocked = false) {
     if (ctx->allocsLeft == 0) return cudaErrorMemoryAllocation;
     if (ctx->allocsLeft > 0) --ctx->allocsLeft;
-    return pageLocked ? cudaMallocHost(p, bytes) : cudaMalloc(p, bytes);
+    const cudaError_t e = pageLocked ? cudaMallocHost(p, bytes) : cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        /* An allocation's failure is not sticky, but it stays the runtime's last error: cleared here, or
+         * the next launch's check would report it. */
+        (void)cudaGetLastError();
+        *p = nullptr;
+    }
+    return e;
 }
 
 extern "C" int artfCudaCreate(int device, ArtfCuda** out) {

@@ -237,6 +237,27 @@ def test_adjoint_rejects_bad_arguments(lib, ctx, torch, scene):
     assert lib.artfCudaHoleAdjoint(ctx, arr2, 1, W, H, None, None, t.data_ptr(), 32, None, None, res, None) != 0
 
 
+def test_adjoint_trail_beyond_the_device_is_refused_cleanly(lib, ctx, torch, scene):
+    """Every state of four 4096 x 4096 views kept would need 620 GB of trail, more than the device holds:
+    the device refuses the allocation, the call returns ARTF_CUDA_ENOMEM before any launch, and the next
+    call on the same context gives the bits it gave before (the refused allocation does not surface as a
+    later launch's error)."""
+    target_p, start = scene
+    target = _rgba(_tangents(lib, ctx, torch, target_p, W, H)[..., 0])
+    before = _adjoint(lib, ctx, torch, [start], target[None], W, H, k=1)
+    n, side = 4, 4096
+    assert n * side * side * 192 * 48 > 2 * torch.cuda.get_device_properties(0).total_memory
+    big = torch.zeros((n, side, side, 4), dtype=torch.float32, device="cuda")  # a full-size target all the same
+    arr = (capi.HoleParams * n)(*([start] * n))
+    res = (capi.AdjointResult * n)()
+    status = lib.artfCudaHoleAdjoint(ctx, arr, n, side, side, None, None, big.data_ptr(), 1, None, None, res, None)
+    assert status == capi.ENOMEM, status
+    del big
+    after = _adjoint(lib, ctx, torch, [start], target[None], W, H, k=1)
+    assert after[0][0] == before[0][0]
+    np.testing.assert_array_equal(after[1], before[1])
+
+
 def test_autograd_function_and_a_short_fit(lib, ctx, torch, scene):
     """The harness's torch.autograd.Function hands back the adjoint's gradient, and Adam on it brings a
     small fit's loss down (to under 60 % of the start's; with a constant rate it may then wander, the
