@@ -39,6 +39,19 @@
 namespace artf {
 
 /* A view as the kernel reads it, from the device view table. */
+/* A value as the unevaluated sum hi + lo of two floats, |lo| at most half an ulp of hi: Dekker's
+ * double-length arithmetic (1971), about 48 significant bits from FP32 instructions, which this GPU
+ * issues 64 times as fast as FP64 ones. */
+struct Ff {
+    float hi, lo;
+};
+
+/* What a ray's set-up under the MOTION guard takes from the view, in double-float: the eye's basis, the
+ * metric's four factors, rho, a and the start terms. */
+struct MotionTermsFf {
+    Ff forward[3], right[3], up[3], metric[4], rho, a, a2, mu0Squared, minusTwoA2;
+};
+
 struct MixedView {
     Frame<float> f;
     Frame<double> d;
@@ -53,6 +66,7 @@ struct MixedView {
     float4* rayOut;
     double wideA2, wideTwoA2; /* a^2 and 2 a^2 in double, for the FP64 sub-steps */
     StartTerms<double> start64; /* what each ray's FP64 set-up takes from the view alone */
+    MotionTermsFf motion;       /* the same, for the set-up of an eye at rest, in double-float */
     float startNarrow[4];     /* the eye's e_r and 1/r in float, where every ray's FP64 set-up starts */
     float wScaleNarrow;       /* -u0^2 sqrt(Delta) sqrt(Sigma), in float: w's factor from the eye */
     float stepBaseNarrow;     /* the step rule's (pi / 24) x step scale, in float */
@@ -137,6 +151,74 @@ __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
     return c;
 }
 
+/* ---- double-float arithmetic --------------------------------------------------------------------------
+ * Sums by Knuth's error-free TwoSum, products by an FMA's residual (the exact error of a rounded product),
+ * each result renormalised by Dekker's fast two-sum; the reciprocal and the reciprocal square root are
+ * the float estimates refined by one Newton-Raphson step in double-float, as this unit's FP64 ones are
+ * refined from float estimates (about 46 and 43 bits).  No step contracts: the only products are the
+ * explicit FMAs. */
+__device__ __forceinline__ Ff ffNorm(float s, float e) {
+    const float hi = s + e;
+    return Ff{hi, e - (hi - s)};
+}
+__device__ __forceinline__ Ff ffAdd(Ff a, Ff b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    return ffNorm(s, ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo));
+}
+__device__ __forceinline__ Ff ffNeg(Ff a) { return Ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ Ff ffSub(Ff a, Ff b) { return ffAdd(a, ffNeg(b)); }
+__device__ __forceinline__ Ff ffMul(Ff a, Ff b) {
+    const float p = a.hi * b.hi;
+    return ffNorm(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p))));
+}
+__device__ __forceinline__ Ff ffMulF(Ff a, float b) {
+    const float p = a.hi * b;
+    return ffNorm(p, fmaf(a.lo, b, fmaf(a.hi, b, -p)));
+}
+__device__ __forceinline__ Ff ffRecip(Ff x) {
+    const float y = 1.f / x.hi;
+    const Ff r = ffSub(Ff{1.f, 0.f}, ffMulF(x, y)); /* 1 - x y */
+    return ffNorm(y, y * r.hi);
+}
+__device__ __forceinline__ Ff ffRsqrt(Ff x) {
+    const float y = rsqrtf(x.hi);
+    const Ff r = ffSub(Ff{1.f, 0.f}, ffMulF(ffMulF(x, y), y)); /* 1 - x y^2 */
+    return ffNorm(y, .5f * y * r.hi);
+}
+/* hi + lo as a double: exact, since the pair holds at most 48 significant bits. */
+__device__ __forceinline__ double ffWide(Ff a) { return widen(a.hi) + widen(a.lo); }
+
+/* The constants of motion alone, for an eye at rest (lens.inc:125-142 without the aberration of
+ * 110-122), in double-float, in rayStartWith's order of operations with the direction normalised first: E,
+ * the axial momentum xi, eta and K = eta + xi^2 and the radial equation's coefficients, rounded to float
+ * (a pair's hi is its value rounded to nearest) into r.c, the five the FP64 sub-steps take into r as
+ * doubles, and the factors the first state is made of (d_x, 1 / (|d| E), across and the axial component
+ * of the direction over E), which the caller forms in FP32 as the reference's integrator has them.  The
+ * FP64 work left is the five doubles' sums. */
+__device__ __forceinline__ void motionConstantsFf(const MotionTermsFf& t, float nx, float ny, MixedRay& r,
+                                                  float& dx, float& over, float& across, float& xiAxis) {
+    Ff d[3];
+    for (int k = 0; k < 3; ++k) d[k] = ffAdd(ffAdd(t.forward[k], ffMulF(t.right[k], nx)), ffMulF(t.up[k], ny));
+    const Ff invLength = ffRsqrt(ffAdd(ffAdd(ffMul(d[0], d[0]), ffMul(d[1], d[1])), ffMul(d[2], d[2])));
+    const Ff dz = ffMul(d[2], invLength);
+    const Ff invEnergy = ffRecip(ffSub(t.metric[0], ffMul(t.metric[1], dz)));
+    const Ff overFf = ffMul(invLength, invEnergy);
+    const Ff xi = ffNeg(ffMul(ffMul(t.metric[2], dz), invEnergy));
+    const Ff xiAxisFf = ffMul(ffMul(t.metric[3], d[2]), overFf);
+    const Ff acrossFf = ffMul(ffMul(t.rho, d[1]), overFf);
+    const Ff eta = ffAdd(ffMul(acrossFf, acrossFf), ffMul(t.mu0Squared, ffSub(ffMul(xiAxisFf, xiAxisFf), t.a2)));
+    const Ff big = ffAdd(eta, ffMul(xi, xi));
+    const Ff uA = ffSub(t.a2, big);
+    const Ff xiOff = ffSub(xi, t.a);
+    const Ff uB = ffMulF(ffAdd(eta, ffMul(xiOff, xiOff)), 3.f);
+    const Ff uC = ffMul(t.minusTwoA2, eta);
+    const Ff xiA = ffMul(xi, t.a);
+    r.c.invEnergy = invEnergy.hi, r.c.xi = xi.hi, r.c.moved = 1.f;
+    r.c.big = big.hi, r.c.uA = uA.hi, r.c.uB = uB.hi, r.c.uC = uC.hi, r.c.xiA = xiA.hi;
+    r.big = ffWide(big), r.uA = ffWide(uA), r.uB = ffWide(uB), r.uC = ffWide(uC), r.xiA = ffWide(xiA);
+    dx = d[0].hi, over = overFf.hi, across = acrossFf.hi, xiAxis = xiAxisFf.hi;
+}
+
 /* The helpers below take the guards apart from the parameters, so that a kernel built for all of them
  * passes a constant and its tests fold away. */
 
@@ -155,19 +237,13 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards
         r.s.u = v.startNarrow[3], r.s.w = narrow(sd.w);
         for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = narrow(sd.v[k]);
     } else if (guards & ARTF_CUDA_GUARD_MOTION) {
-        RayConst<double> cd;
-        MotionFactors<double> m;
-        motionConstants(v.d, v.start64, widen(nx), widen(ny), cd, m);
-        r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi), r.c.moved = 1.f;
-        r.c.big = narrow(cd.big), r.c.uA = narrow(cd.uA), r.c.uB = narrow(cd.uB);
-        r.c.uC = narrow(cd.uC), r.c.xiA = narrow(cd.xiA);
-        r.big = cd.big, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
+        float dx, over, across, xiAxis;
+        motionConstantsFf(v.motion, nx, ny, r, dx, over, across, xiAxis);
         r.c.step = divSqrtR(v.stepBaseNarrow, maxX(r.c.big, 4.f));
         r.step = widen(r.c.step);
         /* (u and n start at the eye's: the view's, narrowed once) */
-        const float across = narrow(m.across), xiAxis = narrow(m.xiAxis);
         r.s.u = v.startNarrow[3];
-        r.s.w = v.wScaleNarrow * narrow(m.dx) * narrow(m.over);
+        r.s.w = v.wScaleNarrow * dx * over;
         for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = across * v.f.etheta[k] + xiAxis * v.f.ephi[k];
     } else {
         rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
@@ -771,6 +847,18 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.startNarrow[3] = (float)v.d.place[2];
     v.wScaleNarrow = (float)v.start64.wScale;
     v.stepBaseNarrow = (float)v.start64.stepBase;
+    auto split = [](double x) {
+        const float hi = (float)x;
+        return Ff{hi, (float)(x - (double)hi)};
+    };
+    for (int k = 0; k < 3; ++k) {
+        v.motion.forward[k] = split(v.d.forward[k]);
+        v.motion.right[k] = split(v.d.right[k]);
+        v.motion.up[k] = split(v.d.up[k]);
+    }
+    for (int k = 0; k < 4; ++k) v.motion.metric[k] = split(v.d.metric[k]);
+    v.motion.rho = split(v.d.place[0]), v.motion.a = split(v.d.a), v.motion.a2 = split(v.start64.a2);
+    v.motion.mu0Squared = split(v.start64.mu0Squared), v.motion.minusTwoA2 = split(v.start64.minusTwoA2);
     v.rhoScale = 1.f / (1.f - v.f.inner / v.f.outer);
     v.uGuard = (float)((double)(l.horizonBand > 0.f ? l.horizonBand : .95f) * frame64.spin[1]);
     v.rays = l.jitter ? l.jitter : (int)(frame.size[2] * frame.size[2]);

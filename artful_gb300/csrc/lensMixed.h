@@ -14,7 +14,7 @@
 namespace artf {
 
 /* A table slot never takes more than this (lensMixed.cu checks it at compile time). */
-constexpr size_t kMixedViewBytesMax = 1152;
+constexpr size_t kMixedViewBytesMax = 1312;
 
 size_t mixedViewBytes();
 /* Fills one table slot; returns the view's unit count and, in *tiles, its 8 x 4 tiles.  rayOut: the

@@ -7,7 +7,7 @@
  * point keeps its only scratch, the batch's view table and its work-queue and tally counters, in one
  * file-scope device array of fixed size, and takes every input and output from the caller.
  *
- * The array lives on every GPU that loads the library until the process exits (74 KB).  Host code
+ * The array lives on every GPU that loads the library until the process exits (82 KB).  Host code
  * cannot use the array's name as a device address, so the first call on each device looks the address
  * up there (cudaGetSymbolAddress, with that device current) and keeps it; after a device reset
  * (cudaDeviceReset, or a reset of the primary context) the kept address is stale, and the process must

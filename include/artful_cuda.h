@@ -334,7 +334,7 @@ void artfCudaBatchGraphDestroy(ArtfCudaGraph* graph);
  * the current device and on the caller's `stream` (a cudaStream_t, or NULL), and every view's map,
  * fluid and hdr must be device pointers the caller owns.  Its scratch (the view table and the queue
  * counters) is one fixed array on each device that loads the library, held until the process exits
- * (74 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
+ * (82 KB): so a batch holds at most ARTF_CUDA_NOALLOC_MAX_VIEWS views, and more is refused with
  * ARTF_CUDA_EINVAL.  No room is left for ray planes or the heavy-first order: each work unit is a pixel,
  * whose rays one lane traces in turn, in pixel order (options->order is ignored), which can be slower
  * than the context's batch for views of several rays a pixel.  The first call on each device looks up
