@@ -300,6 +300,38 @@ template <typename R> ARTF_HD void rayStart(const Frame<R>& f, R nx, R ny, R tim
     rayStartWith(f, startTerms(f, stepScale), nx, ny, time, c, s);
 }
 
+/* The constants of motion alone, for an eye at rest (lens.inc:125-142 without the aberration of
+ * 110-122): E, the axial momentum xi, eta and K = eta + xi^2, the radial equation's coefficients, and the
+ * factors the first state is made of (the ray's unnormalised x component, and across and the axial
+ * component of its direction over E).  The mixed trace evaluates these in double-float pairs, in this
+ * order (motionConstantsFf), and forms the first state and the step from them in FP32, as the reference's
+ * integrator has them; the flop count counts them here. */
+template <typename R> struct MotionFactors {
+    R dx, over, across, xiAxis; /* d_x, 1 / (|d| E), across, xi_axis */
+};
+
+template <typename R> ARTF_HD void motionConstants(const Frame<R>& f, const StartTerms<R>& t, R nx, R ny,
+                                                   RayConst<R>& c, MotionFactors<R>& m) {
+    R d[3];
+    for (int k = 0; k < 3; ++k) d[k] = f.forward[k] + nx * f.right[k] + ny * f.up[k];
+    const R invLength = invSqrtR(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const R dz = d[2] * invLength;
+    const R energy = f.metric[0] - f.metric[1] * dz;
+    c.invEnergy = recipR(energy);
+    m.over = invLength * c.invEnergy;
+    c.xi = R(0) - f.metric[2] * dz * c.invEnergy;
+    m.xiAxis = f.metric[3] * d[2] * m.over;
+    m.across = f.place[0] * d[1] * m.over;
+    const R eta = m.across * m.across + t.mu0Squared * (m.xiAxis * m.xiAxis - t.a2);
+    c.big = eta + c.xi * c.xi;
+    c.uA = t.a2 - c.big;
+    const R xiOff = c.xi - f.a;
+    c.uB = KF(3.) * (eta + xiOff * xiOff);
+    c.uC = t.minusTwoA2 * eta;
+    c.xiA = c.xi * f.a;
+    m.dx = d[0];
+}
+
 /* psi' at u (lens.inc:144 DRAG); the denominator is Delta / r^2, kept off zero. */
 template <typename R> ARTF_HD R dragAt(R a, R a2, R xiA, R x) {
     return divR((-a) * x * (KF(2.) - xiA * x), maxX(R(1) - (x + x) + a2 * x * x, KF(1e-3)));

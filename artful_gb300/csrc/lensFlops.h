@@ -29,15 +29,15 @@
 #define ARTF_FLOPS_ESCAPE 59
 #define ARTF_FLOPS_SKY 58
 
-/* The mixed trace's FP64 work, by the same rule, for the FP64 pipe's roofline:
- *   per set-up   the five constants the FP64 sub-steps take, each the sum of a double-float pair (the
- *                constants of motion themselves are double-float work on the FP32 pipe, the first state
- *                and step FP32 work), and the step's terms in double (formed once a ray)
+/* The mixed trace's wide work, the operations it carries at about FP64's precision, by the same rule:
+ * double-float pairs on the FP32 pipe, but for the horizon's band, which runs in FP64.
+ *   per set-up   a ray's constants of motion (what it takes from its view formed once a view; its first
+ *                state and step are FP32 work), and its step's terms (formed once a ray)
  *   per horizon  one whole radial sub-step (u, du/ds and psi) with those terms given, in the horizon's
  *                band; spin 0: no drag, no psi
  *   per turn     the radial motion alone (u, du/ds), at a turning point of u
  *   per polar    the polar axis component alone (n_z, dn_z/ds), at a turning point of n_z */
-#define ARTF_FLOPS_WIDE_START 11
+#define ARTF_FLOPS_WIDE_START 51
 #define ARTF_FLOPS_WIDE_RADIAL 61
 #define ARTF_FLOPS_WIDE_RADIAL_SPINLESS 34
 #define ARTF_FLOPS_WIDE_TURN 34

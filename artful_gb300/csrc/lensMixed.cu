@@ -1,34 +1,35 @@
-/* artful_cuda — the mixed-precision trace: FP32 for the bulk of each geodesic, FP64 only where
- * stability needs it.
+/* artful_cuda — the mixed-precision trace: FP32 for the bulk of each geodesic, extended precision
+ * (about FP64's) only where stability needs it.  "Wide" work runs as double-float pairs on the FP32 pipe
+ * (Dekker's double-length arithmetic, about 48 bits), or in FP64 where it divides:
  *
  *   MOTION   the constants of motion (E, xi = L_z / E, Carter's eta, K and the radial equation's
- *            coefficients) come from the ray at the eye in FP64, from the frame in double; the first
- *            state's w and v and the step, the integrator's FP32 quantities, are formed from them in
- *            FP32 (the step by the reference's rule from the narrowed K, so every sub-step of a ray,
- *            FP32 or FP64, takes the same one);
+ *            coefficients) come from the ray at the eye in double-float, from the frame's doubles split
+ *            into pairs; the first state's w and v and the step, the integrator's FP32 quantities, are
+ *            formed from them in FP32 (the step by the reference's rule from the rounded K, so every
+ *            sub-step of a ray, FP32 or wide, takes the same one);
  *   HORIZON  within a band of the outer horizon (u > band * 0.995 / r+) the radial sub-step of
  *            (u, du/ds, psi) runs in FP64: Delta / r^2 in the frame-drag rate loses most of its bits to
  *            cancellation there;
  *   RADIAL   the step in which du/ds changes sign (the radial potential's zero) has its motion of
- *            (u, du/ds) in FP64 (psi and its rate, smooth there, stay the FP32 step's);
+ *            (u, du/ds) in double-float (psi and its rate, smooth there, stay the FP32 step's);
  *   POLAR    the step in which the axis part of dn/ds changes sign (the polar potential's zero) has
- *            the axis component (n_z, dn_z/ds) in FP64: n_z'' depends on n_z alone, and the turning
- *            point is its (the components about the axis stay the FP32 step's);
+ *            the axis component (n_z, dn_z/ds) in double-float: n_z'' depends on n_z alone, and the
+ *            turning point is its (the components about the axis stay the FP32 step's);
  *   PSI      psi, the frame-drag angle, is summed with a compensated (two-sum) accumulator, and the
  *            endpoint's Mino time is formed in FP64 from the step count: neither drifts over 192 steps.
  * The radial and polar sub-steps are independent (u'' depends on u alone, n'' on n alone), so a guard
- * costs FP64 only for the part that needs it.  The disc and sky shading stay in FP32.  Built with the
- * fast FP32 flags; in double, + - * are IEEE and / and sqrt are refined hardware estimates (within an
- * ulp or two, lensCore.cuh), as in the plain FP64 trace.
+ * costs wide work only for the part that needs it.  The disc and sky shading stay in FP32.  Built with
+ * the fast FP32 flags; in double, + - * are IEEE and / and sqrt are refined hardware estimates (within
+ * an ulp or two, lensCore.cuh), as in the plain FP64 trace.  At the headline frame the double-float
+ * sub-steps give the FP64 ones' bits, rounded to float, for every pixel.
  *
- * Scheduling (traceMixedQueue): the GB300's FP64 pipe is 1/72 of its FP32 pipe, and a warp pays for an
- * FP64 instruction whatever number of its lanes take part.  So FP64 work runs in warp-wide rounds:
- * lanes that need an FP64 sub-step (or a new ray's FP64 set-up) wait, keeping their FP32 results,
- * while the others keep stepping in FP32; a round runs when `batch` lanes wait, when no lane can move
- * without one, or after a bounded wait.  Pixels of every view of a batch come from one device queue
- * (work stealing across views of uneven size), a lane at a time, by warp ballot and shuffle.  Every
- * lane computes exactly what the per-ray path (traceRayMixed) computes, in the same order: the
- * schedule changes when, never what.  A single frame is a batch of one view. */
+ * Scheduling (traceMixedQueue): a warp pays for a wide sub-step whatever number of its lanes take part.
+ * So wide work runs in warp-wide rounds: lanes that need a wide sub-step (or a new ray's set-up) wait,
+ * keeping their FP32 results, while the others keep stepping in FP32; a round runs when `batch` lanes
+ * wait, when no lane can move without one, or after a bounded wait.  Pixels of every view of a batch
+ * come from one device queue (work stealing across views of uneven size), a lane at a time, by warp
+ * ballot and shuffle.  Every lane computes exactly what the per-ray path (traceRayMixed) computes, in
+ * the same order: the schedule changes when, never what.  A single frame is a batch of one view. */
 #define ARTF_FAST_FP64 1 /* FP64 division and square roots by refined hardware estimates (lensCore.cuh) */
 #define ARTF_FP64_NEWTON_STEPS 1 /* one refinement: ~40 bits, far below float's rounding (3.4 % faster) */
 #include "lensKernel.cuh"
@@ -64,10 +65,10 @@ struct MixedView {
      * unit is one ray and mixedCombine sums each pixel's rays afterwards; without, a unit is a pixel
      * whose rays one lane traces in turn. */
     float4* rayOut;
-    double wideA2, wideTwoA2; /* a^2 and 2 a^2 in double, for the FP64 sub-steps */
-    StartTerms<double> start64; /* what each ray's FP64 set-up takes from the view alone */
-    MotionTermsFf motion;       /* the same, for the set-up of an eye at rest, in double-float */
-    float startNarrow[4];     /* the eye's e_r and 1/r in float, where every ray's FP64 set-up starts */
+    double wideA2;            /* a^2 in double, for the horizon band's FP64 sub-step */
+    StartTerms<double> start64; /* what a moving eye's rays' FP64 set-up takes from the view alone */
+    MotionTermsFf motion;       /* the same and the frame's, for the set-up of an eye at rest, as pairs */
+    float startNarrow[4];     /* the eye's e_r and 1/r in float, where every ray's set-up starts */
     float wScaleNarrow;       /* -u0^2 sqrt(Delta) sqrt(Sigma), in float: w's factor from the eye */
     float stepBaseNarrow;     /* the step rule's (pi / 24) x step scale, in float */
     float rhoScale, uGuard, share;
@@ -98,7 +99,8 @@ struct MixedParams {
 /* One ray's state between steps. */
 struct MixedRay {
     RayConst<float> c;
-    double big, step, uA, uB, uC, xiA; /* the FP64 coefficients the guarded sub-steps use */
+    Ff big, uA, uB, uC, xiA;           /* the coefficients the wide sub-steps use, as double-float pairs */
+    double step;
     RayState<float> s;                 /* s.psi stays 0: a step returns psi's increment */
     float psiHi, psiLo, through, sum[3], hitR, hitPhi;
     int i;
@@ -107,12 +109,12 @@ struct MixedRay {
 };
 
 /* Float <-> double conversions on the integer pipe.  On this GPU a conversion to double costs an FP64
- * instruction and one to float two, on the FP64 pipe that bounds this kernel, while the integer pipe
- * idles: these take a handful of integer instructions instead, for the same bits as the hardware's
- * conversions under this unit's flags (flush-to-zero; round to nearest even), NaN aside (a NaN stays a
- * NaN, its payload is not kept).  artfCudaCheckConversions checks them against the hardware's.  The
- * narrowing is a call, not inlined at its 26 sites in the FP64 paths: inlined, those copies overflowed
- * the instruction cache (warps stalled waiting for instructions; 3.97 ms against 3.50 at 1080p x 4). */
+ * instruction and one to float two, on the narrow FP64 pipe, while the integer pipe idles: these take a
+ * handful of integer instructions instead, for the same bits as the hardware's conversions under this
+ * unit's flags (flush-to-zero; round to nearest even), NaN aside (a NaN stays a NaN, its payload is not
+ * kept).  artfCudaCheckConversions checks them against the hardware's.  The narrowing is a call, not
+ * inlined at its sites in the FP64 paths: inlined, those copies overflowed the instruction cache (warps
+ * stalled waiting for instructions; 3.97 ms against 3.50 at 1080p x 4). */
 __device__ __forceinline__ double widen(float f) {
     const uint32_t b = __float_as_uint(f), sign = b & 0x80000000u, mag = b & 0x7fffffffu, e = mag >> 23;
     uint32_t hi = sign | ((mag >> 3) + 0x38000000u), lo = mag << 29;  /* rebias 127 -> 1023 */
@@ -144,9 +146,11 @@ __device__ __noinline__ float narrow(double d) {
     return __uint_as_float(sign | bits);
 }
 
+__device__ __forceinline__ double ffWide(Ff a);
 __device__ __forceinline__ RayConst<double> wideConst(const MixedRay& r) {
     RayConst<double> c;
-    c.big = r.big, c.step = r.step, c.uA = r.uA, c.uB = r.uB, c.uC = r.uC, c.xiA = r.xiA;
+    c.big = ffWide(r.big), c.step = r.step, c.uA = ffWide(r.uA), c.uB = ffWide(r.uB), c.uC = ffWide(r.uC);
+    c.xiA = ffWide(r.xiA);
     c.invEnergy = c.xi = c.moved = c.time = 0.0; /* (not read by the sub-steps) */
     return c;
 }
@@ -187,14 +191,74 @@ __device__ __forceinline__ Ff ffRsqrt(Ff x) {
 }
 /* hi + lo as a double: exact, since the pair holds at most 48 significant bits. */
 __device__ __forceinline__ double ffWide(Ff a) { return widen(a.hi) + widen(a.lo); }
+__device__ __forceinline__ Ff ffSplit(double x) {
+    const float hi = narrow(x);
+    return Ff{hi, narrow(x - widen(hi))};
+}
+__device__ __forceinline__ Ff ffProd(float a, float b) {
+    const float p = a * b;
+    return Ff{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ Ff ffScale(Ff a, float powerOfTwo) { return Ff{a.hi * powerOfTwo, a.lo * powerOfTwo}; }
+
+/* The step's terms (stepTerms in lensCore.cuh) in double-float from the float step: its square is exact
+ * as a pair, the halves and eighth exact, the sixths products by the float 1/6 as there. */
+struct StepTermsFf {
+    Ff half, eighth, halfSquare, sixthSquare, sixth;
+};
+__device__ __forceinline__ StepTermsFf stepTermsFf(float step) {
+    const Ff step2 = ffProd(step, step);
+    StepTermsFf t;
+    t.half = Ff{step * .5f, 0.f}, t.eighth = ffScale(step2, .125f), t.halfSquare = ffScale(step2, .5f);
+    t.sixthSquare = ffMulF(step2, 1.f / 6.f), t.sixth = ffProd(step, 1.f / 6.f);
+    return t;
+}
+__device__ __forceinline__ StepTerms<double> wideTerms(const StepTermsFf& t) {
+    StepTerms<double> w;
+    w.half = ffWide(t.half), w.eighth = ffWide(t.eighth), w.halfSquare = ffWide(t.halfSquare);
+    w.sixthSquare = ffWide(t.sixthSquare), w.sixth = ffWide(t.sixth);
+    return w;
+}
+/* bendAt: x (uA + x (uB + x uC)) */
+__device__ __forceinline__ Ff ffBend(const MixedRay& r, Ff x) {
+    return ffMul(x, ffAdd(r.uA, ffMul(x, ffAdd(r.uB, ffMul(x, r.uC)))));
+}
+/* radialMotionWith (lensCore.cuh) in double-float, in its order of operations. */
+__device__ __forceinline__ void radialMotionFf(const MixedRay& r, const StepTermsFf& t, float u, float w, Ff& nextU,
+                                               Ff& nextW, Ff& k1) {
+    const Ff uf{u, 0.f};
+    k1 = ffBend(r, uf);
+    const Ff midU = ffAdd(ffAdd(uf, ffMulF(t.half, w)), ffMul(t.eighth, k1));
+    const Ff k2 = ffBend(r, midU);
+    const Ff uw = ffAdd(uf, ffProd(r.c.step, w));
+    const Ff endU = ffAdd(uw, ffMul(t.halfSquare, k2));
+    const Ff k3 = ffBend(r, endU);
+    nextU = ffAdd(uw, ffMul(t.sixthSquare, ffAdd(k1, ffAdd(k2, k2))));
+    nextW = ffAdd(Ff{w, 0.f}, ffMul(t.sixth, ffAdd(ffAdd(k1, k3), ffMulF(k2, 4.f))));
+}
+/* polarAxisWith (lensCore.cuh) in double-float, in its order of operations. */
+__device__ __forceinline__ void polarAxisFf(Ff a2, const MixedRay& r, const StepTermsFf& t, float nz, float vz,
+                                            Ff& nextNz, Ff& nextVz, Ff& a1) {
+    const Ff twoA2 = ffScale(a2, 2.f), nzf{nz, 0.f};
+    const Ff c1 = ffAdd(r.big, ffMul(twoA2, ffProd(nz, nz)));
+    a1 = ffSub(ffMulF(a2, nz), ffMulF(c1, nz));
+    const Ff midN = ffAdd(ffAdd(nzf, ffMulF(t.half, vz)), ffMul(t.eighth, a1));
+    const Ff c2 = ffAdd(r.big, ffMul(twoA2, ffMul(midN, midN)));
+    const Ff a2s = ffSub(ffMul(a2, midN), ffMul(c2, midN));
+    const Ff nv = ffAdd(nzf, ffProd(r.c.step, vz));
+    const Ff endN = ffAdd(nv, ffMul(t.halfSquare, a2s));
+    const Ff c3 = ffAdd(r.big, ffMul(twoA2, ffMul(endN, endN)));
+    const Ff a3 = ffSub(ffMul(a2, endN), ffMul(c3, endN));
+    nextNz = ffAdd(nv, ffMul(t.sixthSquare, ffAdd(a1, ffAdd(a2s, a2s))));
+    nextVz = ffAdd(Ff{vz, 0.f}, ffMul(t.sixth, ffAdd(ffAdd(a1, a3), ffMulF(a2s, 4.f))));
+}
 
 /* The constants of motion alone, for an eye at rest (lens.inc:125-142 without the aberration of
  * 110-122), in double-float, in rayStartWith's order of operations with the direction normalised first: E,
  * the axial momentum xi, eta and K = eta + xi^2 and the radial equation's coefficients, rounded to float
- * (a pair's hi is its value rounded to nearest) into r.c, the five the FP64 sub-steps take into r as
- * doubles, and the factors the first state is made of (d_x, 1 / (|d| E), across and the axial component
- * of the direction over E), which the caller forms in FP32 as the reference's integrator has them.  The
- * FP64 work left is the five doubles' sums. */
+ * (a pair's hi is its value rounded to nearest) into r.c, the five the wide sub-steps take into r as
+ * pairs, and the factors the first state is made of (d_x, 1 / (|d| E), across and the axial component
+ * of the direction over E), which the caller forms in FP32 as the reference's integrator has them. */
 __device__ __forceinline__ void motionConstantsFf(const MotionTermsFf& t, float nx, float ny, MixedRay& r,
                                                   float& dx, float& over, float& across, float& xiAxis) {
     Ff d[3];
@@ -215,14 +279,14 @@ __device__ __forceinline__ void motionConstantsFf(const MotionTermsFf& t, float 
     const Ff xiA = ffMul(xi, t.a);
     r.c.invEnergy = invEnergy.hi, r.c.xi = xi.hi, r.c.moved = 1.f;
     r.c.big = big.hi, r.c.uA = uA.hi, r.c.uB = uB.hi, r.c.uC = uC.hi, r.c.xiA = xiA.hi;
-    r.big = ffWide(big), r.uA = ffWide(uA), r.uB = ffWide(uB), r.uC = ffWide(uC), r.xiA = ffWide(xiA);
+    r.big = big, r.uA = uA, r.uB = uB, r.uC = uC, r.xiA = xiA;
     dx = d[0].hi, over = overFf.hi, across = acrossFf.hi, xiAxis = xiAxisFf.hi;
 }
 
 /* The helpers below take the guards apart from the parameters, so that a kernel built for all of them
  * passes a constant and its tests fold away. */
 
-/* A ray's start: its constants of motion and first state, in FP64 under the MOTION guard. */
+/* A ray's start: its constants of motion and first state, in double-float under the MOTION guard. */
 __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards, const MixedView& v, float nx,
                                            float ny, float time, MixedRay& r) {
     if ((guards & ARTF_CUDA_GUARD_MOTION) && v.d.boost[3] > 1.0) {
@@ -233,7 +297,8 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards
         r.c.invEnergy = narrow(cd.invEnergy), r.c.xi = narrow(cd.xi), r.c.moved = narrow(cd.moved);
         r.c.big = narrow(cd.big), r.c.step = narrow(cd.step), r.c.uA = narrow(cd.uA), r.c.uB = narrow(cd.uB);
         r.c.uC = narrow(cd.uC), r.c.xiA = narrow(cd.xiA);
-        r.big = cd.big, r.step = cd.step, r.uA = cd.uA, r.uB = cd.uB, r.uC = cd.uC, r.xiA = cd.xiA;
+        r.big = ffSplit(cd.big), r.step = cd.step, r.uA = ffSplit(cd.uA), r.uB = ffSplit(cd.uB);
+        r.uC = ffSplit(cd.uC), r.xiA = ffSplit(cd.xiA);
         r.s.u = v.startNarrow[3], r.s.w = narrow(sd.w);
         for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = narrow(sd.v[k]);
     } else if (guards & ARTF_CUDA_GUARD_MOTION) {
@@ -244,10 +309,12 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards
         /* (u and n start at the eye's: the view's, narrowed once) */
         r.s.u = v.startNarrow[3];
         r.s.w = v.wScaleNarrow * dx * over;
-        for (int k = 0; k < 3; ++k) r.s.n[k] = v.startNarrow[k], r.s.v[k] = across * v.f.etheta[k] + xiAxis * v.f.ephi[k];
+        for (int k = 0; k < 3; ++k)
+            r.s.n[k] = v.startNarrow[k], r.s.v[k] = across * v.f.etheta[k] + xiAxis * v.f.ephi[k];
     } else {
         rayStart(v.f, nx, ny, time, p.stepScale, r.c, r.s);
-        r.big = r.c.big, r.step = r.c.step, r.uA = r.c.uA, r.uB = r.c.uB, r.uC = r.c.uC, r.xiA = r.c.xiA;
+        r.big = Ff{r.c.big, 0.f}, r.step = r.c.step, r.uA = Ff{r.c.uA, 0.f}, r.uB = Ff{r.c.uB, 0.f};
+        r.uC = Ff{r.c.uC, 0.f}, r.xiA = Ff{r.c.xiA, 0.f};
     }
     r.c.time = time;
     r.s.psi = 0.f;
@@ -261,7 +328,7 @@ __device__ __forceinline__ void mixedStart(const MixedParams& p, uint32_t guards
     r.lit = false;
 }
 
-/* Which sub-steps of this FP32 step must run again in FP64. */
+/* Which sub-steps of this FP32 step must run again wide. */
 __device__ __forceinline__ void mixedNeeds(uint32_t guards, const MixedView& v, const MixedRay& r,
                                            const StepOut<float>& o, bool& radial, bool& polar, unsigned& reason) {
     const bool band = (guards & ARTF_CUDA_GUARD_HORIZON) && r.s.u > v.uGuard;
@@ -271,34 +338,35 @@ __device__ __forceinline__ void mixedNeeds(uint32_t guards, const MixedView& v, 
     reason = (band ? 1u : 0u) | (turnR && !band ? 2u : 0u) | (polar ? 4u : 0u);
 }
 
-/* The FP64 sub-steps, with the ray's step terms (stepTerms(r.step), formed once a ray).  Radial: in the
- * horizon's band the whole sub-step (the frame-drag rate's Delta / r^2 cancels there); at a turning point
- * of u the motion (u, du/ds) alone, psi and its rate staying the FP32 step's. */
-__device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
-                                           bool band, StepOut<float>& o) {
-    const RayConst<double> c = wideConst(r);
-    double k1;
+/* The wide sub-steps, with the ray's step terms (stepTermsFf, formed once a ray).  Radial: in the
+ * horizon's band the whole sub-step in FP64 (the frame-drag rate's Delta / r^2 cancels there, and it
+ * divides), from the pairs widened; at a turning point of u the motion (u, du/ds) alone in double-float,
+ * psi and its rate staying the FP32 step's. */
+__device__ __forceinline__ void radialWide(const MixedView& v, const MixedRay& r, const StepTermsFf& t, bool band,
+                                           StepOut<float>& o) {
     if (band) {
+        const RayConst<double> c = wideConst(r);
+        double k1;
         RayState<double> s, next;
         s.u = widen(r.s.u), s.w = widen(r.s.w), s.psi = 0.0, s.drag = widen(r.s.drag);
-        radialStepWith(v.d.a, v.wideA2, c, t, s, next, k1);
+        radialStepWith(v.d.a, v.wideA2, c, wideTerms(t), s, next, k1);
         o.next.u = narrow(next.u), o.next.w = narrow(next.w), o.next.psi = narrow(next.psi);
         o.next.drag = narrow(next.drag);
+        o.k1 = narrow(k1);
     } else {
-        double u, w;
-        radialMotionWith(c, t, widen(r.s.u), widen(r.s.w), u, w, k1);
-        o.next.u = narrow(u), o.next.w = narrow(w);
+        Ff u, w, k1;
+        radialMotionFf(r, t, r.s.u, r.s.w, u, w, k1);
+        o.next.u = u.hi, o.next.w = w.hi, o.k1 = k1.hi;
     }
-    o.k1 = narrow(k1);
 }
 
 /* Polar: at the turning point of n_z, the axis component (n_z, dn_z/ds); the components about the axis
  * stay the FP32 step's. */
-__device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, const StepTerms<double>& t,
+__device__ __forceinline__ void polarWide(const MixedView& v, const MixedRay& r, const StepTermsFf& t,
                                           StepOut<float>& o) {
-    double nz, vz, a1z;
-    polarAxisWith(v.wideA2, v.wideTwoA2, wideConst(r), t, widen(r.s.n[2]), widen(r.s.v[2]), nz, vz, a1z);
-    o.next.n[2] = narrow(nz), o.next.v[2] = narrow(vz), o.a1[2] = narrow(a1z);
+    Ff nz, vz, a1z;
+    polarAxisFf(v.motion.a2, r, t, r.s.n[2], r.s.v[2], nz, vz, a1z);
+    o.next.n[2] = nz.hi, o.next.v[2] = vz.hi, o.a1[2] = a1z.hi;
 }
 
 /* After a step: the disc crossing, escape, horizon, opacity and the step cap.  Returns the end's kind
@@ -383,7 +451,7 @@ __device__ __forceinline__ void countReason(unsigned reason, Reasons& n) {
     n.polar += (reason >> 2) & 1u;
 }
 
-/* The per-ray path: one ray from start to end, each step's FP64 sub-steps at once. */
+/* The per-ray path: one ray from start to end, each step's wide sub-steps at once. */
 __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const MixedView& v, float nx, float ny,
                                                   float time, float* sum, ArtfCudaRayEnd* end, Tally& t, Reasons& n) {
     MixedRay r;
@@ -396,7 +464,7 @@ __device__ __forceinline__ unsigned traceRayMixed(const MixedParams& p, const Mi
         unsigned reason;
         mixedNeeds(p.guards, v, r, o, radial, polar, reason);
         if (radial || polar) {
-            const StepTerms<double> terms = stepTerms(r.step);
+            const StepTermsFf terms = stepTermsFf(r.c.step);
             if (radial) radialWide(v, r, terms, (reason & 1u) != 0u, o);
             if (polar) polarWide(v, r, terms, o);
         }
@@ -533,8 +601,8 @@ __global__ void __launch_bounds__(128) placeTiles(const MixedParams p, int total
 constexpr int kInnerSteps = 6;
 
 /* This lane's step terms, from the block's table. */
-__device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256]) {
-    StepTerms<double> t;
+__device__ __forceinline__ StepTermsFf laneTerms(const Ff (*terms)[256]) {
+    StepTermsFf t;
     t.half = terms[0][threadIdx.x], t.eighth = terms[1][threadIdx.x], t.halfSquare = terms[2][threadIdx.x];
     t.sixthSquare = terms[3][threadIdx.x], t.sixth = terms[4][threadIdx.x];
     return t;
@@ -546,9 +614,9 @@ __device__ __forceinline__ StepTerms<double> laneTerms(const double (*terms)[256
 template <bool kOne, bool kAll>
 __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView* one) {
     const uint32_t guards = kAll ? (uint32_t)ARTF_CUDA_GUARD_ALL : p.guards;
-    /* each lane's ray's step terms in double, formed at its set-up: an FP64 round then loads them
-     * where it would multiply them out again (FP64 multiplies are the scarce resource) */
-    __shared__ double terms[5][256];
+    /* each lane's ray's step terms as pairs, formed at its set-up: a wide round then loads them where
+     * it would multiply them out again */
+    __shared__ Ff terms[5][256];
     const unsigned full = 0xFFFFFFFFu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -565,7 +633,7 @@ __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView
     /* Every iteration either advances some lane's ray by a step, starts rays, or ends the loop: the queue
      * is finite and a ray ends within maxSteps steps, so the loop ends. */
     for (;;) {
-        /* (1) refill, batched: the set-up of a ray is FP64 work */
+        /* (1) refill, batched: the set-up of a ray is wide work */
         const unsigned idle = __ballot_sync(full, !live && !exhausted);
         const unsigned liveMask = __ballot_sync(full, live);
         if (idle && (__popc(idle) >= p.refill || liveMask == 0 || sinceStart >= p.maxWait)) {
@@ -615,7 +683,7 @@ __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView
                 /* (the set-up keeps its guard test at run time: made constant there too, the batch ran
                  * 7.61 ms against 7.13, a matter of code layout) */
                 mixedStart(p, p.guards, *v, nx, ny, v->h.disc[2] + v->h.spin[3] * moment, r);
-                const StepTerms<double> t = stepTerms(r.step);
+                const StepTermsFf t = stepTermsFf(r.c.step);
                 terms[0][threadIdx.x] = t.half, terms[1][threadIdx.x] = t.eighth;
                 terms[2][threadIdx.x] = t.halfSquare, terms[3][threadIdx.x] = t.sixthSquare;
                 terms[4][threadIdx.x] = t.sixth;
@@ -626,7 +694,7 @@ __device__ __forceinline__ void mixedQueue(const MixedParams& p, const MixedView
         }
         if (__all_sync(full, exhausted && !live)) break;
 
-        /* (2) FP64 rounds, when enough lanes wait or no other lane can move */
+        /* (2) wide rounds, when enough lanes wait or no other lane can move */
         const unsigned ready = __ballot_sync(full, live && !waitR && !waitP);
         const unsigned needR = __ballot_sync(full, waitR), needP = __ballot_sync(full, waitP);
         if (needR && (__popc(needR) >= p.batch || ready == 0 || sinceRadial >= p.maxWait)) {
@@ -841,7 +909,6 @@ int mixedFillView(const TraceLaunch& l, const ArtfCudaHoleFrame& frame, const Ar
     v.hdr = hdr;
     v.ends = ends;
     v.wideA2 = v.d.a * v.d.a;
-    v.wideTwoA2 = 2.0 * v.wideA2;
     v.start64 = startTerms(v.d, (double)l.stepScale);
     for (int k = 0; k < 3; ++k) v.startNarrow[k] = (float)v.d.er[k];
     v.startNarrow[3] = (float)v.d.place[2];

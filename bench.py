@@ -44,15 +44,18 @@ WORKLOAD = "kerr-hole 1920x1080, 4 jittered rays/px, a=0.998, r_obs=50 M, i=85 d
 # Kernels one mixed frame launches: the tile probe, the heavy-first order, the trace, the ray-plane sum.
 LAUNCHES_PER_MIXED_FRAME = 4
 # DRAM bytes (read + write) of one launch of the mixed trace kernel at this workload, from one ncu
-# capture (dram__bytes_read.sum 17.71 MB + dram__bytes_write.sum 74.34 MB): the map read once, and the
+# capture (dram__bytes_read.sum 17.23 MB + dram__bytes_write.sum 73.95 MB): the map read once, and the
 # part of the 133 MB of ray planes that leaves L2 before the sum reads it back.
-TRACE_TRAFFIC_BYTES = 92_050_000
+TRACE_TRAFFIC_BYTES = 91_173_120
 TRACE_TRAFFIC_GEODESICS = 1920 * 1080 * 4
+FLOPS_WIDE_RADIAL = 61  # lensFlops.h: a whole radial sub-step in the horizon's band (spin != 0)
 # How busy the mixed trace keeps its pipes, from one ncu --set full capture of its kernel at 960x540 x 4
-# (the counted work's fraction above counts an FP64 estimate and its Newton step as one operation): the
-# FP64 pipe's instructions, the FP32 FMA pipe's cycles and the schedulers' issue slots, of peak.
-MIXED_PIPES_BUSY = {"fp64": 0.511, "fp32_fma": 0.317, "issue": 0.660,
-                    "source": "ncu sm__inst_executed_pipe_fp64, sm__pipe_fma_cycles_active, smsp__issue_active "
+# (the counted work above counts a double-float operation, some 3 to 10 FP32 instructions, as one): the
+# FP64 pipe's instructions, the FP32 FMA pipe's cycles, the integer pipe's instructions and the
+# schedulers' issue slots, of peak.
+MIXED_PIPES_BUSY = {"fp64": 0.035, "fp32_fma": 0.398, "alu": 0.370, "issue": 0.690,
+                    "source": "ncu sm__inst_executed_pipe_fp64, sm__pipe_fma_cycles_active, sm__inst_executed_pipe_alu, "
+                              "smsp__issue_active "
                               "of traceMixedQueueOneAll at 960x540 x 4"}
 TRACE_TRAFFIC_SOURCE = "ncu dram__bytes of one launch of the mixed trace kernel at 1920x1080 x 4 jittered rays"
 # The adjoint's checkpoint interval: 32, a ray's state kept every 32 steps and each segment recomputed in
@@ -648,14 +651,16 @@ def main():
             e_ref, img_ref = ends_of(capi.FP64, scale)
             endpoint[label] = endpoint_error(e_mixed, e_ref, img_mixed, img_ref)
 
-    # roofline of the trace: the mixed kernel is bound by the FP64 pipe (its FP64 set-ups and sub-steps:
-    # the pipe is 1/72 of the FP32 one); no tensor cores.  Both pipes' algorithmic work over the step time
+    # roofline of the trace: the mixed kernel runs on the FP32 pipe, its FP32 steps and its wide work (the
+    # set-ups and the turning points as double-float pairs) alike, all but the horizon band's FP64
+    # sub-steps; no tensor cores.  Its algorithmic operations (the FP32 ones and the wide ones, each
+    # counted once) over the step time, against the FP32 pipe's measured peak
     fp32_peak, fp64_peak = C.c_double(), C.c_double()
     capi.check(lib.artfCudaProbePeaks(lib.artfCudaStream(ctx), local, C.byref(fp32_peak), C.byref(fp64_peak)))
-    achieved = s_mixed.flops / (ms_mixed * 1e-3) / 1e12
+    achieved = (s_mixed.flops + s_mixed.flops64) / (ms_mixed * 1e-3) / 1e12
     peak = fp32_peak.value / 1e12
-    achieved64 = s_mixed.flops64 / (ms_mixed * 1e-3) / 1e12
     peak64 = fp64_peak.value / 1e12
+    horizon64 = s_mixed.fp64Horizon * FLOPS_WIDE_RADIAL  # (what still runs on the FP64 pipe)
     # HBM beside it, to show it is not the bound: the trace's DRAM bytes a frame against the measured copy
     traffic = TRACE_TRAFFIC_BYTES * geodesics / TRACE_TRAFFIC_GEODESICS  # (scaled by the rays traced)
     hbm = {"achieved": traffic / (ms_mixed * 1e-3) / 1e9, "unit": "GB/s", "traffic_source": TRACE_TRAFFIC_SOURCE}
@@ -715,13 +720,15 @@ def main():
         "side": side,
         "stratified_2x2": stratified,
         "endpoint_error": endpoint,
-        "roofline": {"bound": "fp64", "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
-                     "frac": achieved64 / peak64, "traffic": traffic,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "measured FMA-chain probe (artfCudaProbePeaks), of measured; "
                                     "MEASURED_PEAKS.json has no FP64- or FP32-pipe figure",
-                     "flops64_per_frame": s_mixed.flops64,
-                     "fp32": {"achieved": achieved, "peak": peak, "frac": achieved / peak,
-                              "flops_per_frame": s_mixed.flops},
+                     "flops_per_frame": s_mixed.flops, "wide_flops_per_frame": s_mixed.flops64,
+                     "fp64": {"achieved": horizon64 / (ms_mixed * 1e-3) / 1e12, "peak": peak64,
+                              "frac": horizon64 / (ms_mixed * 1e-3) / 1e12 / peak64,
+                              "flops_per_frame": horizon64,
+                              "what": "the horizon band's FP64 sub-steps, all that still runs on the FP64 pipe"},
                      "hbm": hbm,
                      "time": "the whole timed step (probe, order, trace, combine)",
                      "pipes_busy": MIXED_PIPES_BUSY},

@@ -232,7 +232,7 @@ typedef struct ArtfCudaRayEnd {
     uint16_t steps;      /* integration steps taken */
     uint8_t crossings;   /* accepted disc crossings */
     uint8_t kind;        /* ARTF_CUDA_END_*, | ARTF_CUDA_END_LIT when a crossing gave light */
-    uint16_t fp64Steps;  /* of those, how many ran in FP64 (the mixed trace) */
+    uint16_t fp64Steps;  /* of those, how many ran wide (the mixed trace) */
     uint16_t reserved;
 } ArtfCudaRayEnd;
 
@@ -250,13 +250,14 @@ enum {
 /* What a trace did, counted on the device. */
 typedef struct ArtfCudaTraceStats {
     uint64_t rays, steps, crossings, escapes, fp64Steps;
-    uint64_t fp64Horizon, fp64Radial, fp64Polar; /* mixed: the FP64 steps by their reason */
-    uint64_t fp64Rounds;                         /* mixed: warp rounds of FP64 steps */
+    uint64_t fp64Horizon, fp64Radial, fp64Polar; /* mixed: the wide (FP64-precision) steps by reason */
+    uint64_t fp64Rounds;                         /* mixed: warp rounds of wide steps */
     double flops;        /* algorithmic FP32-pipe operations (the counting rule is in lensFlops.h) */
     float ms;            /* device time of the trace kernel(s), CUDA events on the context's stream */
     uint32_t bands;      /* launches the frame went out in (ArtfCudaTraceOptions.bandRays) */
-    double flops64;      /* of the work, what ran on the FP64 pipe (FP64: all of flops; mixed: the FP64
-                          * set-ups and sub-steps, by the same rule) */
+    double flops64;      /* of the work, what ran at FP64's precision (FP64: all of flops; mixed: the wide
+                          * set-ups and sub-steps by the same rule, as double-float pairs on the FP32 pipe
+                          * or, in the horizon's band, in FP64) */
 } ArtfCudaTraceStats;
 
 /* Traces one frame into `hdr` (device memory, width * height float4: linear RGB and the class bits).

@@ -92,12 +92,12 @@ int main() {
             RayState<Op> sw, next;
             Op k1, a1[3];
             rayStartWith(f, view, Op(0.1), Op(0.2), Op(0.0), cw, sw);
-            /* (the mixed trace's set-up on the FP64 pipe: the five constants the FP64 sub-steps take, each
-             * the sum of a double-float pair, and the step's terms in double; the constants of motion are
-             * double-float work on the FP32 pipe, and the first state and the step FP32 work) */
-            Op pairs[5];
+            /* (the mixed trace's wide set-up: the constants of motion alone, and the step's terms; the
+             * first state and the step are its FP32 work) */
+            RayConst<Op> cm;
+            MotionFactors<Op> mf;
             g_ops = 0;
-            for (Op& p : pairs) p = Op(1.0) + Op(1e-9);
+            motionConstants(f, view, Op(0.1), Op(0.2), cm, mf);
             const StepTerms<Op> terms = stepTerms(cw.step);
             printf("wide_start%s %ld\n", tag, g_ops);
             g_ops = 0;
