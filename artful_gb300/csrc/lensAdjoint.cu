@@ -736,10 +736,12 @@ struct Trail {
     size_t rays;
 };
 
+/* (streaming stores: the trail, larger than L2, is marked to leave it first, so that the map the forward
+ * kernel shades from stays; 0.182 -> 0.180 ms at 512x288) */
 __device__ __forceinline__ void storeState(float4* at, size_t stride, const RayState<float>& s, float through) {
-    at[0] = make_float4(s.u, s.w, s.n[0], s.n[1]);
-    at[stride] = make_float4(s.n[2], s.v[0], s.v[1], s.v[2]);
-    at[2 * stride] = make_float4(s.psi, s.drag, through, 0.f);
+    __stcs(at, make_float4(s.u, s.w, s.n[0], s.n[1]));
+    __stcs(at + stride, make_float4(s.n[2], s.v[0], s.v[1], s.v[2]));
+    __stcs(at + 2 * stride, make_float4(s.psi, s.drag, through, 0.f));
 }
 
 __device__ __forceinline__ void loadState(const float4* at, size_t stride, RayState<float>& s, float& through) {
