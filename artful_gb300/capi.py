@@ -150,6 +150,7 @@ SIGNATURES = {
                                         _vp, _vp, _vp, _vp, _vp, P(TraceStats)]),
     "artfCudaProbePeaks": (C.c_int, [_vp, C.c_int, P(C.c_double), P(C.c_double)]),
     "artfCudaCheckConversions": (C.c_int, [_vp, C.c_uint64, P(C.c_uint64)]),
+    "artfCudaCheckPairs": (C.c_int, [_vp, _vp, C.c_int, _vp]),
     "artfCudaFailAfter": (C.c_int, [_vp, C.c_int]),
     "artfCudaHoleBatch": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(TraceStats)]),
     "artfCudaBatchGraphCreate": (C.c_int, [_vp, P(View), C.c_int, P(TraceOptions), P(_vp)]),

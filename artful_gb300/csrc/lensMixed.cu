@@ -1008,7 +1008,48 @@ cudaError_t launchMixedTable(const TraceLaunch& l, const void* deviceTable, int 
 
 namespace artf {
 int failWith(int status, const char* message);
+
+namespace {
+/* The pair arithmetic the wide sub-steps use, one record a thread: (a.hi, a.lo, b.hi, b.lo) in,
+ * a + b, a b, 1 / a and 1 / sqrt(|a|) out, each as (hi, lo). */
+__global__ void checkPairs(const float4* in, float* out, int count) {
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= count) return;
+    const float4 r = in[i];
+    const Ff a{r.x, r.y}, b{r.z, r.w};
+    const Ff sum = ffAdd(a, b), product = ffMul(a, b), recip = ffRecip(a);
+    const Ff root = ffRsqrt(Ff{fabsf(a.hi), a.hi < 0.f ? -a.lo : a.lo});
+    float* o = out + (size_t)i * 8;
+    o[0] = sum.hi, o[1] = sum.lo, o[2] = product.hi, o[3] = product.lo;
+    o[4] = recip.hi, o[5] = recip.lo, o[6] = root.hi, o[7] = root.lo;
+}
+}  // namespace
 }  // namespace artf
+
+extern "C" int artfCudaCheckPairs(void* stream, const float* hostIn, int count, float* hostOut) {
+    if (!hostIn || !hostOut || count < 1 || count > (1 << 24))
+        return artf::failWith(ARTF_CUDA_EINVAL, "pairs check: inputs, outputs and 1 .. 2^24 records");
+    const cudaStream_t s = (cudaStream_t)stream;
+    void* buffer = nullptr;
+    const size_t inBytes = sizeof(float) * 4 * (size_t)count, outBytes = sizeof(float) * 8 * (size_t)count;
+    cudaError_t e = cudaMalloc(&buffer, inBytes + outBytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return artf::failWith(ARTF_CUDA_ENOMEM, "pairs check: device allocation");
+    }
+    float4* in = (float4*)buffer;
+    float* out = (float*)((char*)buffer + inBytes);
+    e = cudaMemcpyAsync(in, hostIn, inBytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        artf::checkPairs<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(in, out, count);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hostOut, out, outBytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(buffer);
+    if (e != cudaSuccess) return artf::failWith(ARTF_CUDA_ELAUNCH, cudaGetErrorString(e));
+    return ARTF_CUDA_OK;
+}
 
 extern "C" int artfCudaCheckConversions(void* stream, uint64_t narrowCount, uint64_t* mismatches) {
     if (!mismatches) return artf::failWith(ARTF_CUDA_EINVAL, "mismatches is NULL");

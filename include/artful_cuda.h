@@ -477,6 +477,11 @@ int artfCudaProbePeaks(void* stream, int device, double* fp32Flops, double* fp64
  * rounding ties.  mismatches[0], [1]: differing results of each (two NaNs agree); [2], [3]: the least
  * differing input's bits (all ones: none).  Synchronous on `stream` (a cudaStream_t or NULL). */
 int artfCudaCheckConversions(void* stream, uint64_t narrowCount, uint64_t* mismatches);
+/* The mixed trace's wide sub-steps compute with double-float pairs (hi + lo, about 48 bits) on the FP32
+ * pipe; this runs that arithmetic on `count` records of hostIn (a.hi, a.lo, b.hi, b.lo: host, 4 floats
+ * a record) into hostOut (host, 8 floats a record: a + b, a b, 1 / a and 1 / sqrt(|a|), each hi, lo), for
+ * a test to compare with exact arithmetic.  Synchronous on `stream` (a cudaStream_t or NULL). */
+int artfCudaCheckPairs(void* stream, const float* hostIn, int count, float* hostOut);
 
 #ifdef __cplusplus
 }
