@@ -199,8 +199,8 @@ typedef struct ArtfCudaTraceOptions {
     int compactEvery;    /* steps between warp refills: 0 picks the tuned value */
     int persistent;      /* 1: one block per SM slot, rays pulled from a queue; 0: one ray a thread */
     uint32_t guards;     /* mixed: which FP64 guards run (ARTF_CUDA_GUARD_*); 0 means all */
-    int fp64Batch;       /* mixed: lanes that wait for an FP64 sub-step before a warp runs them; 0: 32 */
-    int refillBatch;     /* mixed: idle lanes before a warp starts new rays (FP64 set-ups); 0: 32 */
+    int fp64Batch;       /* mixed: lanes that wait for a wide sub-step before a warp runs them; 0: 32 */
+    int refillBatch;     /* mixed: idle lanes before a warp starts new rays (wide set-ups); 0: 32 */
     int64_t bandRays;    /* a frame of more rays than this goes out in bands of whole rows of at most this
                           * many rays, each launched and waited for, so that no launch holds the GPU long
                           * (vulkan.c:1729-1756).  0: the reference's choice, bands of 8e6 rays for frames
@@ -214,12 +214,13 @@ typedef struct ArtfCudaTraceOptions {
 
 enum { ARTF_CUDA_ORDER_HEAVY_FIRST = 0, ARTF_CUDA_ORDER_PIXELS = 1 };
 
-/* The mixed trace's FP64 guards. */
+/* The mixed trace's guards: work carried at about FP64's precision ("wide"), as double-float pairs on the
+ * FP32 pipe, or in FP64 within the horizon's band. */
 enum {
-    ARTF_CUDA_GUARD_MOTION = 1,   /* constants of motion and the first state from the ray in FP64 */
-    ARTF_CUDA_GUARD_HORIZON = 2,  /* FP64 steps within the band of the outer horizon */
-    ARTF_CUDA_GUARD_RADIAL = 4,   /* the step where du/ds changes sign, in FP64 */
-    ARTF_CUDA_GUARD_POLAR = 8,    /* the step where the axis part of dn/ds changes sign, in FP64 */
+    ARTF_CUDA_GUARD_MOTION = 1,   /* the constants of motion from the ray, wide (the first state from them) */
+    ARTF_CUDA_GUARD_HORIZON = 2,  /* FP64 radial sub-steps within the band of the outer horizon */
+    ARTF_CUDA_GUARD_RADIAL = 4,   /* the step where du/ds changes sign, its radial motion wide */
+    ARTF_CUDA_GUARD_POLAR = 8,    /* the step where the axis part of dn/ds changes sign, its axis part wide */
     ARTF_CUDA_GUARD_PSI = 16,     /* compensated summation of psi */
     ARTF_CUDA_GUARD_ALL = 31
 };
