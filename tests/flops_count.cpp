@@ -83,7 +83,7 @@ int main() {
         if (f.a != Op(0.0)) s.drag = dragAt(f.a, f.a * f.a, c.xiA, s.u);
         const Op rhoScale = recipR(Op(1.0) - divR(f.inner, f.outer));
         printf("setup%s %ld\n", tag, g_ops);
-        /* the mixed trace's FP64 work: a ray's set-up (what it takes from the view formed once a view,
+        /* the mixed trace's wide work: a ray's set-up (what it takes from the view formed once a view,
          * its step's terms formed once a ray), and one radial and one polar sub-step with those given */
         {
             const StartTerms<Op> view = startTerms(f, Op(1.0));

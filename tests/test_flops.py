@@ -61,9 +61,10 @@ def test_per_escape(counts, constants):
 
 
 def test_mixed_fp64_work(counts, constants):
-    """The mixed trace's FP64 pipe work: a ray's set-up with its view's terms given (and its step's terms
-    formed), a whole radial sub-step (the horizon's band), the radial motion alone (a turning point of u)
-    and the polar axis component alone (a turning point of n_z), with those terms given."""
+    """The mixed trace's wide work (about FP64's precision: double-float pairs, or FP64 in the horizon's
+    band): a ray's set-up with its view's terms given (and its step's terms formed), a whole radial
+    sub-step (the horizon's band), the radial motion alone (a turning point of u) and the polar axis
+    component alone (a turning point of n_z), with those terms given."""
     assert constants["WIDE_START"] == counts["wide_start"] == counts["wide_start_spinless"]
     assert constants["WIDE_RADIAL"] == counts["wide_radial"]
     assert constants["WIDE_RADIAL_SPINLESS"] == counts["wide_radial_spinless"]
